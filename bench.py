@@ -1,0 +1,346 @@
+#!/usr/bin/env python3
+"""Benchmark of the residual-and-update loop (one JSON line on rank 0).
+
+Workload (the 1-GPU configuration of the headline metric): isentropic vortex
+on the periodic box [-5,5]^2, 1024x512 quads with interior nodes jittered by a
+seeded uniform +-0.2h, each quad split along a seeded random diagonal ->
+1,048,576 triangles; LSQ face-neighbour gradients (p=0), no limiter,
+2nd-order upwind reconstruction, Roe flux, 3-stage SSP-RK with a CFL-0.8
+time step.  A "step" is one RK step (3 residual evaluations + updates) over
+all cells; the metric is cell-stage updates/s = ncells * 3 * steps / time.
+
+  value     device-resident steps, CUDA events on the library's stream
+  e2e       the same steps through the C-ABI with the state in pinned host
+            memory: every step uploads U, runs the step, downloads U and the
+            residual norms (all inside the timed region)
+  roofline  dominant kernel: algorithmic bytes per launch / mean launch time
+  cpu_baseline  the CPU oracle (a restatement of the Fortran reference) on
+            the host cores, on a bounded sample of the same workload
+
+--impl reference times the reference's CPU algorithm (the oracle port: the
+Fortran reference cannot be built without a Fortran compiler and MPI) on all
+host threads and prints the same JSON line with "impl": "reference".
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "cell-stage updates/s"
+NX, NY = 1024, 512
+
+
+def workload(precision: int, grad_method: int = 3):
+    import math
+
+    from fvs2d_gb300 import Options, meshgen
+    mesh = meshgen.periodic_square(NX, NY, jitter=0.2, seed=1, jitter_seed=2)
+    opt = Options(vortex=True, vortex_x=0.0, vortex_y=0.0, vortex_kappa=5.0,
+                  vortex_inf=(1.0, 0.5 * math.sqrt(1.4), 0.0, 1.0), grad_method=grad_method, lsq_stencil="fn",
+                  lsq_pow=0.0, limiter=0, reconst=2, rk_nstages=3, rk_order=3, ssprk=True, cfl=0.8, dt_from_cfl=True,
+                  precision=precision)
+    return mesh, opt
+
+
+def config_dict(ncells, nstages, precision_name, extra=None):
+    d = {"workload": f"isentropic vortex, periodic [-5,5]^2, {NX}x{NY} quads jittered +-0.2h, seeded diagonals -> "
+                     f"{ncells} triangles; LSQ-fn p=0, no limiter, 2nd-order upwind, Roe, SSP-RK3, CFL 0.8",
+         "ncells": ncells, "stages_per_step": nstages, "precision": precision_name,
+         "l2_policy": "inputs larger than L2 (device working set > 300 MB vs 129 MB L2)",
+         "parallelism": "replicas (one independent mesh per GPU)"}
+    if extra:
+        d.update(extra)
+    return d
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self, index: int):
+        self.path = tempfile.mktemp(suffix=".csv")
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.f = open(self.path, "w")
+            self.p = subprocess.Popen(["nvidia-smi", f"--id={index}", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                       "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+
+    def stop(self) -> dict:
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        try:
+            self.p.wait(5)
+        except Exception:
+            self.p.kill()
+        self.f.close()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            t = [x.strip() for x in line.split(",")]
+            if len(t) < 9:
+                continue
+            try:
+                sm.append(float(t[1]))
+                mx.append(float(t[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, t[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def traffic_from_profile(kernel: str):
+    """dram bytes per launch of a kernel from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "ncu_traffic.txt")
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        t = line.split()
+        if len(t) >= 3 and not line.startswith("#") and t[0] == kernel:
+            try:
+                return float(t[2])
+            except ValueError:
+                return None
+    return None
+
+
+def algorithmic_bytes(kernel: str, ncells: int, nedges: int, tsize: int) -> float:
+    """Compulsory bytes of one launch (every array read or written once).
+
+    gradient (LSQ-fn, tri): per cell own primitives 4T, stencil ptr 4 +
+      3 ids 12 + 3 coef 6T + 3 weights 3T, gradient out 8T.
+    flux: per edge ids 8 + normal 2T + area T + two offsets 4T, flux*area out
+      4T + ws out T; per cell primitives, gradient and limiter 13T.
+    update: per cell gather list 16 + vol 8 + U 32 read + U0 32 + U 32 write
+      + primitives out 4T; per edge flux slot 5T read once."""
+    T = tsize
+    if kernel == "gradient":
+        return ncells * (4 * T + 16 + 6 * T + 3 * T + 8 * T)
+    if kernel == "flux":
+        return nedges * (8 + 7 * T + 5 * T) + ncells * 13 * T
+    if kernel == "update":
+        return ncells * (16 + 8 + 32 + 32 + 32 + 4 * T) + nedges * 5 * T
+    return 0.0
+
+
+def run_ours(args) -> dict:
+    import numpy as np
+
+    ws, rank, local = dist_env()
+    if ws > 1:
+        os.environ.setdefault("CUDA_VISIBLE_DEVICES", str(local))
+    import torch
+    import torch.distributed as tdist
+
+    from fvs2d_gb300 import PREC_FP64, PREC_FP64_STRICT, PREC_MIXED, Solver, _build
+    _build.build()
+    if ws > 1:
+        tdist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    prec = {"fp64": PREC_FP64, "fp64_strict": PREC_FP64_STRICT, "mixed": PREC_MIXED}[args.precision]
+    mesh, opt = workload(prec)
+    s = Solver(mesh, opt)
+    s.initialize_solution()
+    nc = s.ncells
+    nst = s.sizes.nstages
+    nedges = s.sizes.nedges
+    u_init = s.cvar
+
+    def barrier():
+        torch.cuda.synchronize()
+        if ws > 1:
+            tdist.barrier()
+
+    # warm-up (also derives dt and captures the step graph)
+    s.steps_device(args.warmup)
+    barrier()
+    clk = Clocks(int(os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0]) if ws > 1 else 0)
+    ms = s.steps_device(args.steps)
+    barrier()
+    clocks = clk.stop()
+    t = ms / 1e3
+    if ws > 1:
+        tt = torch.tensor([t], dtype=torch.float64, device="cuda")
+        tdist.all_reduce(tt, op=tdist.ReduceOp.MAX)
+        t = float(tt.item())
+    value = ws * nc * nst * args.steps / t
+
+    # per-kernel timing of one step (CUDA events on the library stream)
+    prof = {}
+    for _ in range(3):
+        for name, m in s.profile_step():
+            prof.setdefault(name, []).append(m)
+    per_launch = {k: statistics.mean(v) for k, v in prof.items()}
+    counts = {k: len(v) // 3 for k, v in prof.items()}
+    total = {k: per_launch[k] * counts[k] for k in per_launch}
+    dom = max(total, key=total.get)
+    tsize = 4 if prec == PREC_MIXED else 8
+    alg = algorithmic_bytes(dom, nc, nedges, tsize)
+    peak, peak_src = measured_peaks()
+    achieved = alg / (per_launch[dom] / 1e3) / 1e9
+    traffic = traffic_from_profile(f"{dom}:{args.precision}")
+    roofline = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 4), "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)",
+                "traffic": traffic, "alg_bytes_per_launch": alg, "mean_launch_ms": round(per_launch[dom], 4),
+                "kernel_share": {k: round(v / sum(total.values()), 4) for k, v in total.items()},
+                "step_bytes_model": "252 B per cell-stage (ideal fused LSQ-fn FP64 stage)",
+                "step_frac_of_hbm": round(value / ws * 252 / (peak * 1e9), 4)}
+
+    # end to end through the C-ABI with pinned host buffers
+    host_u = torch.empty((nc, 4), dtype=torch.float64, pin_memory=True)
+    host_u.numpy()[:] = u_init
+    norms = np.empty((1, 4))
+    e2e_steps = max(3, min(args.steps, 20))
+    s.set_state_ptr(host_u.data_ptr())
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        s.set_state_ptr(host_u.data_ptr())
+        norms = s.time_integration(0.0, 1)
+        s.get_state_ptr(host_u.data_ptr())
+    barrier()
+    te = time.perf_counter() - t0
+    e2e = {"value": ws * nc * nst * e2e_steps / te, "unit": METRIC, "h2d_bytes_per_step": nc * 32,
+           "d2h_bytes_per_step": nc * 32 + norms.nbytes, "steps": e2e_steps,
+           "path": "fvs_set_state + fvs_time_integration(1 step) + fvs_get_state, pinned host memory"}
+
+    launches = s.launches_per_step() * args.steps
+    out = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+           "ms_per_step": t * 1e3 / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+           "dtype": "f64" if prec != PREC_MIXED else "f32 flux/gradient, f64 accumulation/update",
+           "data": "synthetic (seeded mesh generator, analytic vortex initial state)",
+           "config": config_dict(nc, nst, args.precision), "e2e": e2e, "roofline": roofline, "clocks": clocks,
+           "gpu_launches": launches}
+
+    if rank == 0 and args.variants:
+        var = {}
+        for name, pr, gm in (("mixed_lsq", PREC_MIXED, 3), ("fp64_strict_lsq", PREC_FP64_STRICT, 3),
+                             ("fp64_ggcb", PREC_FP64, 1), ("fp64_ggnb", PREC_FP64, 2), ("mixed_ggnb", PREC_MIXED, 2)):
+            m2, o2 = workload(pr, gm)
+            with Solver(m2, o2) as s2:
+                s2.initialize_solution()
+                s2.steps_device(3)
+                vms = s2.steps_device(10)
+                var[name] = {"value": s2.ncells * s2.sizes.nstages * 10 / (vms / 1e3), "ms_per_step": vms / 10}
+        out["variants"] = var
+    if rank == 0 and not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline(mesh, opt, budget_s=args.cpu_budget)
+    s.close()
+    if ws > 1:
+        tdist.destroy_process_group()
+    return out if rank == 0 else None
+
+
+def host_threads() -> int:
+    try:
+        return len(os.sched_getaffinity(0))
+    except Exception:
+        return os.cpu_count() or 1
+
+
+def cpu_baseline(mesh, opt, budget_s: float = 12.0, nthreads: int | None = None) -> dict:
+    """The oracle on the host cores: a bounded number of full-mesh steps."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from oracle_lib import Oracle
+    nthreads = nthreads or host_threads()
+    orc = Oracle(mesh, opt, nthreads=nthreads)
+    orc.initialize_solution()
+    t0 = time.perf_counter()
+    orc.time_integration(0.0, 1)
+    t1 = time.perf_counter() - t0
+    k = int(max(1, min(50, budget_s / max(t1, 1e-6))))
+    t0 = time.perf_counter()
+    orc.time_integration(0.0, k)
+    t = time.perf_counter() - t0
+    nst = orc.sizes.nstages
+    return {"value": orc.ncells * nst * k / t, "unit": METRIC, "cores": nthreads, "kind": "port",
+            "sample": f"{k} full SSP-RK3 steps of the {orc.ncells}-cell mesh (after 1 untimed step), "
+                      f"race-free OpenMP oracle with {nthreads} threads",
+            "seconds": round(t, 3)}
+
+
+def run_reference(args) -> dict | None:
+    ws, rank, local = dist_env()
+    if rank != 0:
+        return None
+    from fvs2d_gb300 import PREC_FP64
+    mesh, opt = workload(PREC_FP64)
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from oracle_lib import Oracle
+    nth = host_threads()
+    orc = Oracle(mesh, opt, nthreads=nth)
+    orc.initialize_solution()
+    for _ in range(max(1, min(args.warmup, 1))):
+        orc.time_integration(0.0, 1)
+    # each timed step is one full RK step of the whole mesh; bound the count
+    # so the run ends within a few minutes
+    t0 = time.perf_counter()
+    orc.time_integration(0.0, 1)
+    t1 = time.perf_counter() - t0
+    k = int(max(1, min(args.steps, 60.0 / max(t1, 1e-6))))
+    t0 = time.perf_counter()
+    orc.time_integration(0.0, k)
+    t = time.perf_counter() - t0
+    nc, nst = orc.ncells, orc.sizes.nstages
+    v = nc * nst * k / t
+    sample = (f"{k} full SSP-RK3 steps of the {nc}-cell mesh on {nth} host threads (race-free OpenMP restatement "
+              f"of the Fortran reference; the reference itself needs a Fortran compiler and MPI)")
+    return {"metric": METRIC, "value": v, "unit": METRIC, "n_gpus": ws, "steps": k, "warmup": args.warmup,
+            "ms_per_step": t * 1e3 / k, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded mesh generator, analytic vortex initial state)",
+            "config": config_dict(nc, nst, "fp64"), "impl": "reference",
+            "cpu_baseline": {"value": v, "unit": METRIC, "cores": nth, "kind": "port", "sample": sample},
+            "e2e": {"value": v, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "fp64_strict", "mixed"])
+    ap.add_argument("--no-variants", dest="variants", action="store_false")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-budget", type=float, default=12.0)
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "ours":
+        args.warmup = 3
+    out = run_reference(args) if args.impl == "reference" else run_ours(args)
+    if out is not None:
+        print(json.dumps(out), flush=True)
+
+
+if __name__ == "__main__":
+    main()

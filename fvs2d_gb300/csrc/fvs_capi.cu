@@ -1,0 +1,864 @@
+// fvs_capi.cu — the C-ABI of include/fvs2d.h: handle life cycle, device
+// layout (reverse Cuthill-McKee cell order, edge slots, gather lists), the
+// per-step CUDA graph and the host<->device copies.
+//
+// Reference procedures replaced (see include/fvs2d.h for the mapping):
+//   compute_residual   src/residual.f90:23-177   -> fvs_residual
+//   time_integration   src/runge_kutta.f90:94-114 -> fvs_time_integration
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <deque>
+#include <memory>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "fvs_internal.hpp"
+
+using namespace fvs;
+
+namespace {
+
+thread_local std::string g_create_error;
+
+struct DevBuf {
+  void* p = nullptr;
+  size_t n = 0;
+};
+
+__global__ void k_scatter_in(const double* __restrict__ ref, const int* __restrict__ perm, double* __restrict__ dev, int nc) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nc) return;
+  const double2* s = reinterpret_cast<const double2*>(ref) + 2 * (size_t)i;
+  double2* t = reinterpret_cast<double2*>(dev) + 2 * (size_t)perm[i];
+  t[0] = s[0];
+  t[1] = s[1];
+}
+
+__global__ void k_gather_out(const double* __restrict__ dev, const int* __restrict__ perm, double* __restrict__ ref, int nc,
+                             int width) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nc) return;
+  for (int k = 0; k < width; k++) ref[(size_t)width * i + k] = dev[(size_t)width * perm[i] + k];
+}
+
+template <typename T>
+__global__ void k_gather_out_t(const T* __restrict__ dev, const int* __restrict__ perm, double* __restrict__ ref, int nc, int width) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nc) return;
+  for (int k = 0; k < width; k++) ref[(size_t)width * i + k] = double(dev[(size_t)width * perm[i] + k]);
+}
+
+}  // namespace
+
+struct fvs_handle {
+  HostMesh hm;
+  fvs_options o;
+  double pvar_inf[4];
+  std::string err;
+  const KernelSet* ks = nullptr;
+  bool mixed = false;
+  cudaStream_t stream = nullptr;
+  std::vector<void*> allocs;
+  DevView d;
+  std::vector<int> perm;   // reference cell -> device cell
+  int* d_perm = nullptr;   // device copy of perm
+  double* d_stage = nullptr;  // [nc][4] reference-order staging
+  double* h_small = nullptr;  // pinned scratch for control words
+  std::vector<StageParams> stages;
+  double dt = 0;
+  bool dt_ready = false;
+  cudaGraphExec_t graph = nullptr;
+  int graph_steps = 0;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  int nblk = 0;
+  int launches_per_step = 0;
+  bool host_only = false;
+
+  ~fvs_handle() {
+    if (graph) cudaGraphExecDestroy(graph);
+    if (ev0) cudaEventDestroy(ev0);
+    if (ev1) cudaEventDestroy(ev1);
+    for (void* p : allocs) cudaFree(p);
+    if (h_small) cudaFreeHost(h_small);
+    if (stream) cudaStreamDestroy(stream);
+  }
+
+  int fail(int code, const std::string& msg) {
+    err = msg;
+    return code;
+  }
+  int cuda_fail(cudaError_t e, const char* where) {
+    err = std::string(where) + ": " + cudaGetErrorString(e);
+    return FVS_ERR_CUDA;
+  }
+  template <typename V>
+  bool upload(V*& dst, const std::vector<V>& src) {
+    dst = nullptr;
+    if (src.empty()) return true;
+    void* p = nullptr;
+    if (cudaMalloc(&p, sizeof(V) * src.size()) != cudaSuccess) return false;
+    allocs.push_back(p);
+    if (cudaMemcpy(p, src.data(), sizeof(V) * src.size(), cudaMemcpyHostToDevice) != cudaSuccess) return false;
+    dst = static_cast<V*>(p);
+    return true;
+  }
+  bool alloc(void*& dst, size_t bytes) {
+    dst = nullptr;
+    if (bytes == 0) bytes = 16;
+    if (cudaMalloc(&dst, bytes) != cudaSuccess) return false;
+    allocs.push_back(dst);
+    return cudaMemset(dst, 0, bytes) == cudaSuccess;
+  }
+};
+
+namespace {
+
+// reverse Cuthill-McKee over face neighbours: BFS from a pseudo-peripheral
+// cell, neighbours visited by increasing degree, order reversed.
+std::vector<int> rcm_order(const HostMesh& h) {
+  const int nc = h.nc;
+  std::vector<int> deg(nc, 0);
+  for (int ic = 0; ic < nc; ic++)
+    for (int k = 0; k < h.nvrt[ic]; k++) deg[ic] += h.nghbr[4 * ic + k] >= 0;
+  std::vector<int> order;
+  order.reserve(nc);
+  std::vector<char> seen(nc, 0);
+  std::vector<int> level(nc, -1);
+  auto bfs_last = [&](int s) {
+    // farthest cell of minimum degree from s (one sweep)
+    std::vector<int> q{s};
+    std::fill(level.begin(), level.end(), -1);
+    level[s] = 0;
+    for (size_t i = 0; i < q.size(); i++) {
+      int c = q[i];
+      for (int k = 0; k < h.nvrt[c]; k++) {
+        int n = h.nghbr[4 * c + k];
+        if (n >= 0 && level[n] < 0) { level[n] = level[c] + 1; q.push_back(n); }
+      }
+    }
+    int best = q.back();
+    for (int c : q)
+      if (level[c] == level[q.back()] && deg[c] < deg[best]) best = c;
+    return best;
+  };
+  int next_unseen = 0;
+  while ((int)order.size() < nc) {
+    while (seen[next_unseen]) next_unseen++;
+    int start = next_unseen;
+    for (int ic = next_unseen; ic < nc; ic++)
+      if (!seen[ic] && deg[ic] < deg[start]) start = ic;
+    start = bfs_last(bfs_last(start));
+    size_t head = order.size();
+    order.push_back(start);
+    seen[start] = 1;
+    int nb[4];
+    while (head < order.size()) {
+      int c = order[head++];
+      int m = 0;
+      for (int k = 0; k < h.nvrt[c]; k++) {
+        int n = h.nghbr[4 * c + k];
+        if (n >= 0 && !seen[n]) nb[m++] = n;
+      }
+      std::sort(nb, nb + m, [&](int a, int b) { return deg[a] != deg[b] ? deg[a] < deg[b] : a < b; });
+      for (int i = 0; i < m; i++) {
+        seen[nb[i]] = 1;
+        order.push_back(nb[i]);
+      }
+    }
+  }
+  std::reverse(order.begin(), order.end());
+  std::vector<int> perm(nc);
+  for (int i = 0; i < nc; i++) perm[order[i]] = i;
+  return perm;
+}
+
+inline double minimg(double d, double L) { return L > 0 ? d - L * std::nearbyint(d / L) : d; }
+
+template <typename T>
+std::vector<T> conv(const std::vector<double>& v) {
+  return std::vector<T>(v.begin(), v.end());
+}
+
+// Builds every device array of the handle from the host mesh.
+template <typename T>
+int build_device(fvs_handle* H) {
+  HostMesh& h = H->hm;
+  DevView& d = H->d;
+  const int nc = h.nc;
+  H->perm = rcm_order(h);
+  const std::vector<int>& perm = H->perm;
+  std::vector<int> iperm(nc);
+  for (int i = 0; i < nc; i++) iperm[perm[i]] = i;
+  const int nint = (int)h.edge_intr.size(), nbe = (int)h.b_edge.size();
+  d.nc = nc;
+  d.nint = nint;
+  d.nedge = nint + nbe;
+  // interior edge slots sorted by their first device cell (stable)
+  std::vector<int> eorder(nint);
+  std::iota(eorder.begin(), eorder.end(), 0);
+  std::stable_sort(eorder.begin(), eorder.end(), [&](int a, int b) {
+    int ea = h.edge_intr[a], eb = h.edge_intr[b];
+    int ka = std::min(perm[h.ec1[ea]], perm[h.ec2[ea]]), kb = std::min(perm[h.ec1[eb]], perm[h.ec2[eb]]);
+    return ka < kb;
+  });
+  std::vector<int> slot_of_intr(nint);
+  for (int s = 0; s < nint; s++) slot_of_intr[eorder[s]] = s;
+  const int ne = d.nedge;
+  std::vector<int2> ecell(ne);
+  std::vector<T> enrm(2 * (size_t)ne), earea(ne), edL(2 * (size_t)ne), edR(2 * (size_t)std::max(nint, 1));
+  std::vector<int> ebtype(std::max(nbe, 1));
+  std::vector<T> exy(2 * (size_t)std::max(nbe, 1));
+  for (int s = 0; s < nint; s++) {
+    int ie = h.edge_intr[eorder[s]];
+    int L = h.ec1[ie], R = h.ec2[ie];
+    ecell[s] = make_int2(perm[L], perm[R]);
+    enrm[2 * s] = T(h.enx[ie]); enrm[2 * s + 1] = T(h.eny[ie]);
+    earea[s] = T(h.ea[ie]);
+    edL[2 * s] = T(minimg(h.ex[ie] - h.xc[L], h.Lx)); edL[2 * s + 1] = T(minimg(h.ey[ie] - h.yc[L], h.Ly));
+    edR[2 * s] = T(minimg(h.ex[ie] - h.xc[R], h.Lx)); edR[2 * s + 1] = T(minimg(h.ey[ie] - h.yc[R], h.Ly));
+  }
+  // boundary edges in the reference's processing order; edge i of boundary
+  // ib is paired with bndry(ib)%cell(i) (src/residual.f90:114-125)
+  std::vector<int> bcell_of(nbe);
+  for (int ib = 0, k = 0; ib < h.nb; ib++)
+    for (int i = h.b_eptr[ib]; i < h.b_eptr[ib + 1]; i++, k++) {
+      int ie = h.b_edge[i], L = h.b_cell[h.b_cptr[ib] + (i - h.b_eptr[ib])], s = nint + k;
+      bcell_of[k] = L;
+      ecell[s] = make_int2(perm[L], -1);
+      enrm[2 * s] = T(h.enx[ie]); enrm[2 * s + 1] = T(h.eny[ie]);
+      earea[s] = T(h.ea[ie]);
+      edL[2 * s] = T(minimg(h.ex[ie] - h.xc[L], h.Lx)); edL[2 * s + 1] = T(minimg(h.ey[ie] - h.yc[L], h.Ly));
+      ebtype[k] = h.b_type[ib];
+      exy[2 * k] = T(h.ex[ie]); exy[2 * k + 1] = T(h.ey[ie]);
+    }
+  // gather lists in the reference's summation order: interior edges in
+  // edge_intr order (+ to c1, - to c2), then boundary edges
+  std::vector<int4> cf(nc, make_int4(0, 0, 0, 0));
+  std::vector<int> ncf(nc, 0);
+  auto push = [&](int cell, int v) -> bool {
+    int dc = perm[cell];
+    if (ncf[dc] >= 4) return false;
+    int* p = reinterpret_cast<int*>(&cf[dc]);
+    p[ncf[dc]++] = v;
+    return true;
+  };
+  for (int i = 0; i < nint; i++) {
+    int ie = h.edge_intr[i], s = slot_of_intr[i];
+    if (!push(h.ec1[ie], s + 1) || !push(h.ec2[ie], -(s + 1))) return H->fail(FVS_ERR_MESH, "a cell has more than 4 flux contributions");
+  }
+  for (int k = 0; k < nbe; k++)
+    if (!push(bcell_of[k], nint + k + 1)) return H->fail(FVS_ERR_MESH, "a cell has more than 4 flux contributions");
+  // cell arrays in device order
+  std::vector<double> vol(nc), rvol(nc);
+  std::vector<T> eps2(nc), cpos(8 * (size_t)nc, T(0));
+  std::vector<int8_t> nvrt(nc);
+  for (int o = 0; o < nc; o++) {
+    int dc = perm[o];
+    vol[dc] = h.vol[o];
+    rvol[dc] = 1.0 / h.vol[o];
+    eps2[dc] = T(h.eps2[o]);
+    nvrt[dc] = h.nvrt[o];
+    for (int k = 0; k < h.nvrt[o]; k++) {
+      int je = h.cedge[4 * o + k];
+      cpos[8 * dc + 2 * k] = T(minimg(h.ex[je] - h.xc[o], h.Lx));
+      cpos[8 * dc + 2 * k + 1] = T(minimg(h.ey[je] - h.yc[o], h.Ly));
+    }
+  }
+  // stencils in device order, per-cell entry order kept
+  std::vector<int> st_ptr(nc + 1, 0), st_cell;
+  std::vector<T> st_coef, st_w, coef0, coefedg;
+  std::vector<int8_t> st_node;
+  const bool ggnb = h.grad_method == FVS_GRAD_GGNB;
+  for (int dc = 0; dc < nc; dc++) {
+    int o = iperm[dc];
+    for (int k = h.st_ptr[o]; k < h.st_ptr[o + 1]; k++) {
+      st_cell.push_back(perm[h.st_cell[k]]);
+      if (ggnb) {
+        st_coef.push_back(T(h.st_coef[k]));
+        st_node.push_back(h.st_node[k]);
+      } else {
+        st_coef.push_back(T(h.st_coef[2 * k]));
+        st_coef.push_back(T(h.st_coef[2 * k + 1]));
+      }
+      if (!h.st_w.empty()) st_w.push_back(T(h.st_w[k]));
+    }
+    st_ptr[dc + 1] = (int)st_cell.size();
+  }
+  if (!h.coef0.empty()) {
+    coef0.resize(2 * (size_t)nc);
+    for (int o = 0; o < nc; o++) { coef0[2 * perm[o]] = T(h.coef0[2 * o]); coef0[2 * perm[o] + 1] = T(h.coef0[2 * o + 1]); }
+  }
+  if (!h.coefedg.empty()) {
+    coefedg.resize(8 * (size_t)nc);
+    for (int o = 0; o < nc; o++)
+      for (int k = 0; k < 8; k++) coefedg[8 * perm[o] + k] = T(h.coefedg[8 * o + k]);
+  }
+  // upload
+  bool ok = true;
+  double *dvol, *drvol;
+  int4* dcf;
+  int8_t *dnv, *dsn;
+  int *dsp, *dsc, *deb, *dperm;
+  int2* dec;
+  T *t_eps2, *t_cpos, *t_coef, *t_w, *t_c0, *t_ce, *t_nrm, *t_area, *t_edL, *t_edR, *t_exy;
+  ok = ok && H->upload(dvol, vol) && H->upload(drvol, rvol) && H->upload(dcf, cf) && H->upload(dnv, nvrt);
+  ok = ok && H->upload(dsp, st_ptr) && H->upload(dsc, st_cell) && H->upload(dsn, st_node) && H->upload(dec, ecell);
+  ok = ok && H->upload(deb, ebtype) && H->upload(dperm, perm);
+  ok = ok && H->upload(t_eps2, eps2) && H->upload(t_cpos, cpos) && H->upload(t_coef, st_coef) && H->upload(t_w, st_w);
+  ok = ok && H->upload(t_c0, coef0) && H->upload(t_ce, coefedg) && H->upload(t_nrm, enrm) && H->upload(t_area, earea);
+  ok = ok && H->upload(t_edL, edL) && H->upload(t_edR, edR) && H->upload(t_exy, exy);
+  H->d_perm = dperm;
+  if (!ok) return H->fail(FVS_ERR_NOMEM, "device allocation or upload of the mesh failed");
+  d.vol = dvol; d.rvol = drvol; d.cflist = dcf; d.nvrt = dnv; d.st_ptr = dsp; d.st_cell = dsc; d.st_node = dsn;
+  d.ecell = dec; d.ebtype = deb; d.eps2 = t_eps2; d.cpos = t_cpos; d.st_coef = t_coef; d.st_w = t_w; d.coef0 = t_c0;
+  d.coefedg = t_ce; d.enrm = t_nrm; d.earea = t_area; d.edL = t_edL; d.edR = t_edR; d.exy = t_exy;
+  // state and work arrays
+  void* p;
+  const size_t n4 = 4 * (size_t)nc;
+  H->nblk = (nc + 255) / 256;
+  d.nblk_red = H->nblk;
+  d.norm_cap = 4096;
+#define FVS_ALLOC(field, type, bytes) ok = ok && H->alloc(p, bytes); d.field = static_cast<type>(p)
+  FVS_ALLOC(U, double*, 8 * n4);
+  FVS_ALLOC(U0, double*, 8 * n4);
+  FVS_ALLOC(F, double*, 8 * n4);
+  FVS_ALLOC(resid, double*, 8 * n4);
+  FVS_ALLOC(ws, double*, 8 * (size_t)nc);
+  FVS_ALLOC(dtl, double*, 8 * (size_t)nc);
+  FVS_ALLOC(Pv, void*, sizeof(T) * n4);
+  FVS_ALLOC(Gx, void*, sizeof(T) * n4);
+  FVS_ALLOC(Gy, void*, sizeof(T) * n4);
+  FVS_ALLOC(phi, void*, sizeof(T) * (size_t)nc);
+  FVS_ALLOC(eflux, void*, sizeof(T) * 4 * (size_t)ne);
+  FVS_ALLOC(ews, void*, sizeof(T) * (size_t)ne);
+  FVS_ALLOC(partials, double*, 32 * (size_t)H->nblk);
+  FVS_ALLOC(norms, double*, 32 * (size_t)d.norm_cap);
+  FVS_ALLOC(stepctl, int*, 16);
+  FVS_ALLOC(tctl, double*, 16);
+#undef FVS_ALLOC
+  ok = ok && H->alloc(p, 8 * n4);
+  H->d_stage = static_cast<double*>(p);
+  if (!ok) return H->fail(FVS_ERR_NOMEM, "device allocation of the state failed");
+  // phi: 0 for first order, 1 without a limiter (src/gradient_limiter.f90:30-40)
+  std::vector<T> phi0(nc, T(H->o.reconst == FVS_RECON_UPWIND1 ? 0.0 : 1.0));
+  if (cudaMemcpy(d.phi, phi0.data(), sizeof(T) * nc, cudaMemcpyHostToDevice) != cudaSuccess)
+    return H->fail(FVS_ERR_CUDA, "phi upload failed");
+  return FVS_OK;
+}
+
+void set_stages(fvs_handle* H) {
+  const fvs_options& o = H->o;
+  double hr[5], c[5], dts[5];
+  rk_coefficients(o, H->dt, hr, c, dts);
+  H->stages.clear();
+  const int ns = o.rk_nstages;
+  for (int k = 1; k <= ns; k++) {
+    StageParams sp;
+    sp.stage = k; sp.nstages = ns; sp.steady = o.steady; sp.last = (k == ns);
+    sp.mode = (ns == 3 && o.ssprk) ? MODE_SSP3 : (o.ssprk ? MODE_SSP42 : MODE_RK);
+    sp.h = hr[k]; sp.coef = c[k]; sp.dts = dts[k];
+    if (sp.mode == MODE_SSP42) sp.cst = (k == 4) ? 1.0 / 4.0 : 1.0 / 3.0;             // :380-381
+    else if (sp.mode == MODE_RK) sp.cst = (k == 3) ? 1.0 : (k == 4 ? 1.0 / 6.0 : 1.0 / 2.0);  // :300-302
+    else sp.cst = 1.0;
+    if (sp.mode == MODE_SSP3) {
+      static const double A[4] = {0, 0.0, 0.75, 1.0 / 3.0}, B[4] = {0, 1.0, 0.25, 2.0 / 3.0};
+      sp.a = A[k]; sp.b = B[k];
+    }
+    H->stages.push_back(sp);
+  }
+  H->d.dt = H->dt;
+}
+
+void enqueue_step(fvs_handle* H) {
+  const KernelSet& K = *H->ks;
+  cudaStream_t s = H->stream;
+  K.begin_step(H->d, s);
+  for (const StageParams& sp : H->stages) {
+    K.gradient(H->d, s);
+    K.flux(H->d, sp.dts, s);
+    K.update(H->d, sp, s);
+  }
+  K.norm_final(H->d, s);
+}
+
+int count_launches(const fvs_handle* H) {
+  int per_stage = (H->d.first_order ? 0 : 1) + 2;
+  return 2 + per_stage * (int)H->stages.size();
+}
+
+int ensure_graph(fvs_handle* H, int steps_per_graph) {
+  if (H->graph && H->graph_steps == steps_per_graph) return FVS_OK;
+  if (H->graph) { cudaGraphExecDestroy(H->graph); H->graph = nullptr; }
+  cudaGraph_t g;
+  cudaError_t e = cudaStreamBeginCapture(H->stream, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) return H->cuda_fail(e, "cudaStreamBeginCapture");
+  for (int i = 0; i < steps_per_graph; i++) enqueue_step(H);
+  e = cudaStreamEndCapture(H->stream, &g);
+  if (e != cudaSuccess) return H->cuda_fail(e, "cudaStreamEndCapture");
+  e = cudaGraphInstantiate(&H->graph, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return H->cuda_fail(e, "cudaGraphInstantiate");
+  H->graph_steps = steps_per_graph;
+  return FVS_OK;
+}
+
+int check_launch(fvs_handle* H, const char* where) {
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? FVS_OK : H->cuda_fail(e, where);
+}
+
+// residual of the current device state at `time` (stage-free): fills d.resid, d.ws
+int device_residual(fvs_handle* H, double time) {
+  H->h_small[0] = time;
+  cudaError_t e = cudaMemcpyAsync(H->d.tctl + 1, H->h_small, sizeof(double), cudaMemcpyHostToDevice, H->stream);
+  if (e != cudaSuccess) return H->cuda_fail(e, "time upload");
+  H->ks->cvar2pvar(H->d, H->stream);
+  H->ks->gradient(H->d, H->stream);
+  H->ks->flux(H->d, 0.0, H->stream);
+  H->ks->residual_out(H->d, H->stream);
+  return check_launch(H, "residual kernels");
+}
+
+int ensure_dt(fvs_handle* H, double t1) {
+  if (H->dt_ready) return FVS_OK;
+  if (H->o.dt_from_cfl && !H->o.steady) {
+    int rc = device_residual(H, t1);
+    if (rc) return rc;
+    std::vector<double> ws(H->hm.nc);
+    cudaError_t e = cudaMemcpyAsync(ws.data(), H->d.ws, sizeof(double) * ws.size(), cudaMemcpyDeviceToHost, H->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(H->stream);
+    if (e != cudaSuccess) return H->cuda_fail(e, "ws download");
+    double dmin = 0.0;
+    for (int o = 0; o < H->hm.nc; o++) {
+      double dd = H->o.cfl * H->hm.vol[o] / (0.5 * ws[H->perm[o]]);
+      if (o == 0 || dd < dmin) dmin = dd;
+    }
+    H->dt = dmin;
+  }
+  set_stages(H);
+  if (H->graph) { cudaGraphExecDestroy(H->graph); H->graph = nullptr; }
+  H->dt_ready = true;
+  return FVS_OK;
+}
+
+int state_in(fvs_handle* H, const double* cvar) {
+  const size_t bytes = 32 * (size_t)H->hm.nc;
+  cudaError_t e = cudaMemcpyAsync(H->d_stage, cvar, bytes, cudaMemcpyHostToDevice, H->stream);
+  if (e != cudaSuccess) return H->cuda_fail(e, "state upload");
+  k_scatter_in<<<(H->hm.nc + 255) / 256, 256, 0, H->stream>>>(H->d_stage, H->d_perm, H->d.U, H->hm.nc);
+  H->ks->cvar2pvar(H->d, H->stream);
+  return check_launch(H, "state scatter");
+}
+
+int state_out(fvs_handle* H, const double* dev, double* host, int width) {
+  const int nc = H->hm.nc;
+  k_gather_out<<<(nc + 255) / 256, 256, 0, H->stream>>>(dev, H->d_perm, H->d_stage, nc, width);
+  cudaError_t e = cudaMemcpyAsync(host, H->d_stage, sizeof(double) * width * (size_t)nc, cudaMemcpyDeviceToHost, H->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(H->stream);
+  return e == cudaSuccess ? FVS_OK : H->cuda_fail(e, "state download");
+}
+
+template <typename T>
+int typed_out(fvs_handle* H, const void* dev, double* host, int width) {
+  const int nc = H->hm.nc;
+  k_gather_out_t<T><<<(nc + 255) / 256, 256, 0, H->stream>>>(static_cast<const T*>(dev), H->d_perm, H->d_stage, nc, width);
+  cudaError_t e = cudaMemcpyAsync(host, H->d_stage, sizeof(double) * width * (size_t)nc, cudaMemcpyDeviceToHost, H->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(H->stream);
+  return e == cudaSuccess ? FVS_OK : H->cuda_fail(e, "array download");
+}
+
+int validate_options(const fvs_options* o, std::string& err) {
+  if (o->flux != 1) { err = "only the Roe flux (1) exists (src/input.f90:269-277)"; return FVS_ERR_INVALID; }
+  if (o->grad_method < 1 || o->grad_method > 3) { err = "grad_method must be 1, 2 or 3"; return FVS_ERR_INVALID; }
+  if (o->limiter < 0 || o->limiter > 3) { err = "limiter must be 0..3"; return FVS_ERR_INVALID; }
+  if (o->reconst < 1 || o->reconst > 3) { err = "reconst must be 1..3"; return FVS_ERR_INVALID; }
+  if (o->limiter != FVS_LIM_NONE && o->grad_method != FVS_GRAD_LSQ && o->reconst != FVS_RECON_UPWIND1) {
+    err = "the limiter reads the LSQ stencil (src/gradient_limiter.f90:54): use LSQ gradients";
+    return FVS_ERR_INVALID;
+  }
+  const int ns = o->rk_nstages;
+  bool ok = (ns == 4 && o->rk_order >= 1 && o->rk_order <= 4 && (!o->ssprk || o->rk_order == 2)) || (ns == 3 && o->ssprk);
+  if (!ok) { err = "RK coefficients exist for 4 stages (SSP: order 2) and the SSP-RK3 extension only"; return FVS_ERR_INVALID; }
+  if (o->precision < 0 || o->precision > 2) { err = "precision must be 0, 1 or 2"; return FVS_ERR_INVALID; }
+  if (!(o->gamma > 1.0)) { err = "gamma must be > 1"; return FVS_ERR_INVALID; }
+  return FVS_OK;
+}
+
+}  // namespace
+
+// ===========================================================================
+// C-ABI
+// ===========================================================================
+extern "C" {
+
+int fvs_options_default(fvs_options* o) {
+  if (!o) return FVS_ERR_INVALID;
+  std::memset(o, 0, sizeof(*o));
+  o->gamma = 1.4; o->mach_inf = 0.5; o->aoa_inf_deg = 0.0; o->dt = 0.01; o->cfl = 1.0;
+  o->steady = 0; o->vortex = 0; o->ntstart = 1;
+  o->grad_method = FVS_GRAD_LSQ; o->lsq_stencil = FVS_LSQ_FN; o->lsq_pow = 0.0;
+  o->limiter = FVS_LIM_NONE; o->reconst = FVS_RECON_UPWIND2; o->umuscl = 0.0; o->flux = 1;
+  o->rk_nstages = 4; o->rk_order = 4; o->ssprk = 0;
+  o->vortex_x = 5.0; o->vortex_y = 5.0; o->vortex_kappa = 1.0;
+  o->vortex_inf[0] = 1.0; o->vortex_inf[1] = 0.2; o->vortex_inf[2] = 0.0; o->vortex_inf[3] = 1.0;
+  o->dt_from_cfl = 0; o->precision = FVS_PREC_FP64; o->diverge_factor = 0.0;
+  return FVS_OK;
+}
+
+int fvs_create(const fvs_mesh* mesh, const fvs_options* opt, fvs_handle** out) {
+  if (!out) return FVS_ERR_INVALID;
+  *out = nullptr;
+  if (!mesh || !opt || mesh->nnodes <= 0 || mesh->ncells_tri < 0 || mesh->ncells_quad < 0 ||
+      mesh->ncells_tri + mesh->ncells_quad <= 0 || !mesh->node_xy || (mesh->ncells_tri && !mesh->tri_nodes) ||
+      (mesh->ncells_quad && !mesh->quad_nodes) || mesh->nbndries < 0 ||
+      (mesh->nbndries && (!mesh->bndry_ncells || !mesh->bndry_type || !mesh->bndry_cells))) {
+    g_create_error = "invalid mesh description";
+    return FVS_ERR_INVALID;
+  }
+  std::string err;
+  int rc = validate_options(opt, err);
+  if (rc) { g_create_error = err; return rc; }
+  std::unique_ptr<fvs_handle> H(new fvs_handle());
+  H->o = *opt;
+  if (H->o.reconst != FVS_RECON_UMUSCL) H->o.umuscl = 0.0;  // src/input.f90:250,254
+  rc = build_host_mesh(mesh, &H->o, H->hm, err);
+  if (rc) { g_create_error = err; return rc; }
+  // free stream, src/data_solution.f90:55-63
+  const double aoa = H->o.aoa_inf_deg * 3.141592653589793238462643383279502884 / 180.0;
+  H->pvar_inf[0] = 1.0;
+  H->pvar_inf[1] = H->o.mach_inf * std::cos(aoa);
+  H->pvar_inf[2] = H->o.mach_inf * std::sin(aoa);
+  H->pvar_inf[3] = 1.0 / H->o.gamma;
+  H->mixed = H->o.precision == FVS_PREC_MIXED;
+  H->ks = H->o.precision == FVS_PREC_FP64_STRICT ? &kernels_fp64_strict()
+          : H->mixed ? &kernels_mixed() : &kernels_fp64_fast();
+  cudaError_t e = cudaStreamCreateWithFlags(&H->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) { g_create_error = std::string("cudaStreamCreate: ") + cudaGetErrorString(e); return FVS_ERR_CUDA; }
+  if (cudaMallocHost(&H->h_small, 64) != cudaSuccess) { g_create_error = "pinned allocation failed"; return FVS_ERR_NOMEM; }
+  cudaEventCreate(&H->ev0);
+  cudaEventCreate(&H->ev1);
+  DevView& d = H->d;
+  d.gamma = H->o.gamma;
+  d.khalf = H->o.umuscl / 2.0;
+  d.nkhalf = -H->o.umuscl / 2.0;
+  d.omk = 1.0 - H->o.umuscl;
+  d.cfl = H->o.cfl;
+  d.limiter = H->o.limiter;
+  d.grad_method = H->o.grad_method;
+  d.first_order = H->o.reconst == FVS_RECON_UPWIND1;
+  d.vortex = H->o.vortex;
+  d.vx = H->o.vortex_x; d.vy = H->o.vortex_y; d.vkappa = H->o.vortex_kappa;
+  for (int k = 0; k < 4; k++) { d.vinf[k] = H->o.vortex_inf[k]; d.pinf[k] = H->pvar_inf[k]; }
+  mms_constants(d.mc);
+  rc = H->mixed ? build_device<float>(H.get()) : build_device<double>(H.get());
+  if (rc) { g_create_error = H->err; return rc; }
+  H->dt = H->o.dt;
+  // steady runs start from dt_local = dt (src/runge_kutta.f90:73-76)
+  {
+    std::vector<double> dtl(H->hm.nc, H->o.dt);
+    cudaMemcpy(d.dtl, dtl.data(), 8 * dtl.size(), cudaMemcpyHostToDevice);
+  }
+  if (!(H->o.dt_from_cfl && !H->o.steady)) {
+    set_stages(H.get());
+    H->dt_ready = true;
+  } else {
+    set_stages(H.get());
+  }
+  H->launches_per_step = count_launches(H.get());
+  e = cudaDeviceSynchronize();
+  if (e != cudaSuccess) { g_create_error = std::string("setup: ") + cudaGetErrorString(e); return FVS_ERR_CUDA; }
+  *out = H.release();
+  return FVS_OK;
+}
+
+int fvs_create_host(const fvs_mesh* mesh, const fvs_options* opt, fvs_handle** out) {
+  if (!out) return FVS_ERR_INVALID;
+  *out = nullptr;
+  if (!mesh || !opt || mesh->nnodes <= 0 || mesh->ncells_tri < 0 || mesh->ncells_quad < 0 ||
+      mesh->ncells_tri + mesh->ncells_quad <= 0 || !mesh->node_xy || (mesh->ncells_tri && !mesh->tri_nodes) ||
+      (mesh->ncells_quad && !mesh->quad_nodes) || mesh->nbndries < 0 ||
+      (mesh->nbndries && (!mesh->bndry_ncells || !mesh->bndry_type || !mesh->bndry_cells))) {
+    g_create_error = "invalid mesh description";
+    return FVS_ERR_INVALID;
+  }
+  std::string err;
+  int rc = validate_options(opt, err);
+  if (rc) { g_create_error = err; return rc; }
+  std::unique_ptr<fvs_handle> H(new fvs_handle());
+  H->o = *opt;
+  if (H->o.reconst != FVS_RECON_UMUSCL) H->o.umuscl = 0.0;
+  rc = build_host_mesh(mesh, &H->o, H->hm, err);
+  if (rc) { g_create_error = err; return rc; }
+  H->host_only = true;
+  H->dt = H->o.dt;
+  *out = H.release();
+  return FVS_OK;
+}
+
+void fvs_destroy(fvs_handle* h) { delete h; }
+
+const char* fvs_last_error(const fvs_handle* h) { return h ? h->err.c_str() : g_create_error.c_str(); }
+
+int fvs_get_sizes(const fvs_handle* h, fvs_sizes* s) {
+  if (!h || !s) return FVS_ERR_INVALID;
+  const HostMesh& m = h->hm;
+  std::memset(s, 0, sizeof(*s));
+  s->nnodes = m.nnodes; s->ncells = m.nc; s->ncells_tri = m.ntri; s->ncells_quad = m.nquad;
+  s->nedges = m.ne; s->nedges_intr = (int)m.edge_intr.size(); s->nedges_bndr = (int)m.edge_bndr.size();
+  s->ncells_intr = (int)m.cell_intr.size(); s->ncells_bndr = (int)m.cell_bndr.size(); s->nbndries = m.nb;
+  s->stencil_len = (int)m.st_cell.size(); s->nstages = h->o.rk_nstages;
+  s->heff1 = m.heff1; s->heff2 = m.heff2; s->vol_sum = m.vol1; s->vol_green = m.vol2; s->dt = h->dt;
+  return FVS_OK;
+}
+
+int fvs_export_size(const fvs_handle* h, const char* name, int64_t* nbytes) {
+  if (!h || !name || !nbytes) return FVS_ERR_INVALID;
+  return export_array(h->hm, name, nullptr, nbytes);
+}
+
+int fvs_export(const fvs_handle* h, const char* name, void* dst, int64_t nbytes) {
+  if (!h || !name || !dst) return FVS_ERR_INVALID;
+  return export_array(h->hm, name, dst, &nbytes);
+}
+
+int fvs_init_state(fvs_handle* h) {
+  if (h && h->host_only) return h->fail(FVS_ERR_INVALID, "host-only handle (fvs_create_host) has no device state");
+  if (!h) return FVS_ERR_INVALID;
+  // initialize_solution, src/initialize.f90:19-90 (ntstart <= 1)
+  const int nc = h->hm.nc;
+  std::vector<double> cv(4 * (size_t)nc);
+  const double g = h->o.gamma, t0 = double(h->o.ntstart - 1) * h->o.dt;
+  for (int ic = 0; ic < nc; ic++) {
+    double pv[4];
+    if (h->o.ntstart < 1) std::memcpy(pv, &h->hm.mms_sol[4 * ic], sizeof pv);
+    else if (h->o.vortex) vortex_state(h->o, t0, h->hm.xc[ic], h->hm.yc[ic], pv);
+    else std::memcpy(pv, h->pvar_inf, sizeof pv);
+    double* u = &cv[4 * ic];
+    u[0] = pv[0];
+    u[1] = pv[0] * pv[1];
+    u[2] = pv[0] * pv[2];
+    u[3] = pv[3] / (g - 1.0) + 0.5 * pv[0] * (pv[1] * pv[1] + pv[2] * pv[2]);
+  }
+  return fvs_set_state(h, cv.data());
+}
+
+int fvs_set_state(fvs_handle* h, const double* cvar) {
+  if (h && h->host_only) return h->fail(FVS_ERR_INVALID, "host-only handle (fvs_create_host) has no device state");
+  if (!h || !cvar) return FVS_ERR_INVALID;
+  int rc = state_in(h, cvar);
+  if (rc) return rc;
+  cudaError_t e = cudaStreamSynchronize(h->stream);
+  return e == cudaSuccess ? FVS_OK : h->cuda_fail(e, "set_state");
+}
+
+int fvs_get_state(fvs_handle* h, double* cvar) {
+  if (h && h->host_only) return h->fail(FVS_ERR_INVALID, "host-only handle (fvs_create_host) has no device state");
+  if (!h || !cvar) return FVS_ERR_INVALID;
+  return state_out(h, h->d.U, cvar, 4);
+}
+
+int fvs_residual(fvs_handle* h, double time, double* resid, double* ws_nrml) {
+  if (h && h->host_only) return h->fail(FVS_ERR_INVALID, "host-only handle (fvs_create_host) has no device state");
+  if (!h) return FVS_ERR_INVALID;
+  int rc = device_residual(h, time);
+  if (rc) return rc;
+  if (resid && (rc = state_out(h, h->d.resid, resid, 4))) return rc;
+  if (ws_nrml && (rc = state_out(h, h->d.ws, ws_nrml, 1))) return rc;
+  cudaError_t e = cudaStreamSynchronize(h->stream);
+  return e == cudaSuccess ? FVS_OK : h->cuda_fail(e, "residual");
+}
+
+int fvs_get_gradient(fvs_handle* h, double* grad, double* phi) {
+  if (h && h->host_only) return h->fail(FVS_ERR_INVALID, "host-only handle (fvs_create_host) has no device state");
+  if (!h) return FVS_ERR_INVALID;
+  const int nc = h->hm.nc;
+  int rc = FVS_OK;
+  if (grad) {
+    if (h->mixed) {
+      if ((rc = typed_out<float>(h, h->d.Gx, grad, 4))) return rc;
+      if ((rc = typed_out<float>(h, h->d.Gy, grad + 4 * (size_t)nc, 4))) return rc;
+    } else {
+      if ((rc = typed_out<double>(h, h->d.Gx, grad, 4))) return rc;
+      if ((rc = typed_out<double>(h, h->d.Gy, grad + 4 * (size_t)nc, 4))) return rc;
+    }
+  }
+  if (phi) rc = h->mixed ? typed_out<float>(h, h->d.phi, phi, 1) : typed_out<double>(h, h->d.phi, phi, 1);
+  return rc;
+}
+
+static int run_steps(fvs_handle* h, double t1, int nsteps, double* resnorm, float* ms) {
+  int rc = ensure_dt(h, t1);
+  if (rc) return rc;
+  if ((rc = ensure_graph(h, 1))) return rc;
+  // control words: t1, steps done = 0
+  h->h_small[0] = t1;
+  reinterpret_cast<int*>(h->h_small + 1)[0] = 0;
+  cudaError_t e = cudaMemcpyAsync(h->d.tctl, h->h_small, sizeof(double), cudaMemcpyHostToDevice, h->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(h->d.stepctl, h->h_small + 1, sizeof(int), cudaMemcpyHostToDevice, h->stream);
+  if (e != cudaSuccess) return h->cuda_fail(e, "step control upload");
+  if (ms) cudaEventRecord(h->ev0, h->stream);
+  const int cap = h->d.norm_cap;
+  int done = 0;
+  while (done < nsteps) {
+    int chunk = std::min(cap, nsteps - done);
+    for (int i = 0; i < chunk; i++) {
+      e = cudaGraphLaunch(h->graph, h->stream);
+      if (e != cudaSuccess) return h->cuda_fail(e, "cudaGraphLaunch");
+    }
+    if (resnorm) {
+      e = cudaMemcpyAsync(resnorm + 4 * (size_t)done, h->d.norms, 32 * (size_t)chunk, cudaMemcpyDeviceToHost, h->stream);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+      if (e != cudaSuccess) return h->cuda_fail(e, "norm download");
+    }
+    done += chunk;
+  }
+  if (ms) {
+    cudaEventRecord(h->ev1, h->stream);
+    e = cudaEventSynchronize(h->ev1);
+    if (e != cudaSuccess) return h->cuda_fail(e, "event sync");
+    cudaEventElapsedTime(ms, h->ev0, h->ev1);
+  }
+  e = cudaStreamSynchronize(h->stream);
+  if (e != cudaSuccess) return h->cuda_fail(e, "time integration");
+  if (resnorm)
+    for (size_t i = 0; i < 4 * (size_t)nsteps; i++)
+      if (!std::isfinite(resnorm[i])) return h->fail(FVS_ERR_NONFINITE, "residual norm is not finite at step " + std::to_string(i / 4 + 1));
+  return FVS_OK;
+}
+
+int fvs_time_integration(fvs_handle* h, double t1, int32_t nsteps, double* resnorm) {
+  if (h && h->host_only) return h->fail(FVS_ERR_INVALID, "host-only handle (fvs_create_host) has no device state");
+  if (!h || nsteps < 0) return FVS_ERR_INVALID;
+  if (nsteps == 0) return FVS_OK;
+  return run_steps(h, t1, nsteps, resnorm, nullptr);
+}
+
+int fvs_run_to_drop(fvs_handle* h, double t1, int32_t max_steps, double drop, int32_t check_every, int32_t* steps_done,
+                    double* resnorm) {
+  if (h && h->host_only) return h->fail(FVS_ERR_INVALID, "host-only handle (fvs_create_host) has no device state");
+  if (!h || max_steps <= 0 || check_every <= 0) return FVS_ERR_INVALID;
+  std::vector<double> buf(4 * (size_t)max_steps);
+  double first = 0;
+  int done = 0;
+  int rc = FVS_OK;
+  while (done < max_steps) {
+    int n = std::min(check_every, max_steps - done);
+    double tstart = t1 + double(done) * h->dt;
+    rc = run_steps(h, tstart, n, buf.data() + 4 * (size_t)done, nullptr);
+    if (done == 0 && rc == FVS_OK) first = buf[0];
+    done += n;
+    if (rc) break;
+    double last = buf[4 * (size_t)(done - 1)];
+    if (h->o.diverge_factor > 0 && last > h->o.diverge_factor * first) {
+      rc = h->fail(FVS_ERR_DIVERGED, "residual grew past diverge_factor");
+      break;
+    }
+    bool hit = false;
+    int at = done;
+    for (int i = done - n; i < done; i++)
+      if (buf[4 * (size_t)i] <= drop * first) { hit = true; at = i + 1; break; }
+    if (hit) { done = at; break; }
+  }
+  if (steps_done) *steps_done = done;
+  if (resnorm) std::memcpy(resnorm, buf.data(), 32 * (size_t)done);
+  return rc;
+}
+
+int fvs_vortex_error(fvs_handle* h, double time, double* e) {
+  if (h && h->host_only) return h->fail(FVS_ERR_INVALID, "host-only handle (fvs_create_host) has no device state");
+  if (!h || !e) return FVS_ERR_INVALID;
+  const HostMesh& m = h->hm;
+  std::vector<double> cv(4 * (size_t)m.nc);
+  int rc = fvs_get_state(h, cv.data());
+  if (rc) return rc;
+  // error_isentropic_vortex, src/mms.f90:271-365
+  const double g = h->o.gamma;
+  double mx[4] = {0, 0, 0, 0}, l1[4] = {0, 0, 0, 0}, l2[4] = {0, 0, 0, 0}, L2 = 0;
+  for (int ic : m.cell_intr) {
+    double pv[4], ex[4], d[4];
+    vortex_state(h->o, time, m.xc[ic], m.yc[ic], pv);
+    ex[0] = pv[0]; ex[1] = pv[0] * pv[1]; ex[2] = pv[0] * pv[2];
+    ex[3] = pv[3] / (g - 1.0) + 0.5 * ex[0] * (pv[1] * pv[1] + pv[2] * pv[2]);
+    for (int v = 0; v < 4; v++) {
+      d[v] = std::fabs(cv[4 * ic + v] - ex[v]);
+      if (d[v] > mx[v]) mx[v] = d[v];
+      l1[v] = l1[v] + d[v];
+      l2[v] = l2[v] + d[v] * d[v];
+    }
+    L2 = L2 + d[0] * d[0] + d[1] * d[1] + d[2] * d[2] + d[3] * d[3];
+  }
+  const double n = double(m.cell_intr.size());
+  for (int v = 0; v < 4; v++) { e[3 * v] = mx[v]; e[3 * v + 1] = l1[v] / n; e[3 * v + 2] = std::sqrt(l2[v] / n); }
+  e[12] = std::sqrt(L2 / n);
+  return FVS_OK;
+}
+
+int fvs_mms_source(fvs_handle* h, double* src) {
+  if (!h || !src) return FVS_ERR_INVALID;
+  std::memcpy(src, h->hm.mms_src.data(), sizeof(double) * h->hm.mms_src.size());
+  return FVS_OK;
+}
+
+int fvs_steps_device(fvs_handle* h, int32_t nsteps, float* ms) {
+  if (h && h->host_only) return h->fail(FVS_ERR_INVALID, "host-only handle (fvs_create_host) has no device state");
+  if (!h || nsteps <= 0) return FVS_ERR_INVALID;
+  return run_steps(h, 0.0, nsteps, nullptr, ms);
+}
+
+int fvs_profile_step(fvs_handle* h, int32_t cap, int32_t* n, char* names, float* ms) {
+  if (h && h->host_only) return h->fail(FVS_ERR_INVALID, "host-only handle (fvs_create_host) has no device state");
+  if (!h || !n || !names || !ms) return FVS_ERR_INVALID;
+  int rc = ensure_dt(h, 0.0);
+  if (rc) return rc;
+  const KernelSet& K = *h->ks;
+  cudaStream_t s = h->stream;
+  std::vector<cudaEvent_t> ev;
+  std::vector<std::string> nm;
+  auto mark = [&](const std::string& label) {
+    cudaEvent_t x;
+    cudaEventCreate(&x);
+    cudaEventRecord(x, s);
+    ev.push_back(x);
+    nm.push_back(label);
+  };
+  mark("start");
+  K.begin_step(h->d, s);
+  for (const StageParams& sp : h->stages) {
+    K.gradient(h->d, s);
+    mark("gradient");
+    K.flux(h->d, sp.dts, s);
+    mark("flux");
+    K.update(h->d, sp, s);
+    mark("update");
+  }
+  K.norm_final(h->d, s);
+  mark("norm");
+  cudaError_t e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return h->cuda_fail(e, "profile step");
+  int m = 0;
+  for (size_t i = 1; i < ev.size() && m < cap; i++, m++) {
+    std::snprintf(names + 32 * m, 32, "%s", nm[i].c_str());
+    cudaEventElapsedTime(&ms[m], ev[i - 1], ev[i]);
+  }
+  for (cudaEvent_t x : ev) cudaEventDestroy(x);
+  *n = m;
+  return FVS_OK;
+}
+
+int fvs_launches_per_step(const fvs_handle* h, int32_t* n) {
+  if (!h || !n) return FVS_ERR_INVALID;
+  *n = h->launches_per_step;
+  return FVS_OK;
+}
+
+int fvs_device_state(fvs_handle* h, void** dptr) {
+  if (h && h->host_only) return h->fail(FVS_ERR_INVALID, "host-only handle (fvs_create_host) has no device state");
+  if (!h || !dptr) return FVS_ERR_INVALID;
+  *dptr = h->d.U;
+  return FVS_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,154 @@
+// fvs_internal.hpp — structures shared by the host setup (fvs_setup.cpp),
+// the C-ABI (fvs_capi.cpp) and the device kernels (fvs_kernels.cuh).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/fvs2d.h"
+
+namespace fvs {
+
+// ---------------------------------------------------------------------------
+// Host mesh in the reference's numbering, 0-based, "-1" where the reference
+// stores 0 (no neighbour / boundary).  Built by build_host_mesh() so that
+// every connectivity and geometry array is bit-identical to grid_data
+// (src/grid_procs.f90:170-794) and the gradient setups.
+// ---------------------------------------------------------------------------
+struct HostMesh {
+  int nnodes = 0, ntri = 0, nquad = 0, nc = 0;
+  double Lx = 0, Ly = 0, xmin = 0, ymin = 0;
+  std::vector<double> xn, yn;
+  std::vector<int8_t> nvrt;
+  std::vector<int> cnode;     // [nc][4]
+  std::vector<int> nghbr;     // [nc][4]
+  std::vector<int> nghbre;    // [nc][4]
+  std::vector<int> cedge;     // [nc][4]
+  std::vector<double> nrmlsign;  // [nc][4]
+  std::vector<double> xc, yc, vol;
+  std::vector<int> nd_ptr, nd_cell;  // node -> cells, in ascending cell order
+  int ne = 0;
+  std::vector<int> en1, en2, ec1, ec2;
+  std::vector<double> ex, ey, ea, enx, eny, etx, ety;
+  std::vector<int> cell_intr, cell_bndr, edge_intr, edge_bndr, bedge_cell;
+  int nb = 0;
+  std::vector<int> b_type, b_cptr, b_cell, b_eptr, b_edge;  // CSR per boundary
+  double heff1 = 0, heff2 = 0, vol1 = 0, vol2 = 0;
+  // gradient operator (reference order)
+  int grad_method = 0;
+  std::vector<int> st_ptr, st_cell;  // CSR
+  std::vector<double> st_coef;       // LSQ/GGCB: [len][2]; GGNB: [len]
+  std::vector<double> st_w;          // LSQ weights
+  std::vector<int8_t> st_node;       // GGNB: local node of each entry
+  std::vector<double> coef0;         // GGCB/GGNB [nc][2]
+  std::vector<double> coefedg;       // GGNB [nc][4][2]
+  std::vector<double> eps2;          // limiter eps^2 per cell
+  std::vector<double> mms_sol, mms_src;  // [nc][4]
+};
+
+// options derived once per handle
+struct Scheme {
+  fvs_options o;
+  double pvar_inf[4];
+  double mc[16];  // MMS constants
+  double h_rk[5], rk_coef[5], dts[5];
+};
+
+int build_host_mesh(const fvs_mesh* m, const fvs_options* o, HostMesh& hm, std::string& err);
+void mms_constants(double* mc);
+void mms_euler2d(const double* mc, double gamma, double xc, double yc, double* sol, double* rhs);
+void vortex_state(const fvs_options& o, double t, double x, double y, double* pv);
+void rk_coefficients(const fvs_options& o, double dt, double* h_rk, double* rk_coef, double* dts);
+int export_array(const HostMesh& hm, const char* name, void* dst, int64_t* nbytes);
+
+// ---------------------------------------------------------------------------
+// Device view.  Arrays are in device order (cells renumbered by reverse
+// Cuthill-McKee, interior edges sorted by their first device cell, boundary
+// edges after them in the reference's processing order).  "T" arrays hold the
+// compute type of the path: double for FP64, float for MIXED.
+// ---------------------------------------------------------------------------
+enum StageMode : int {
+  MODE_RK = 0,        // time_integ_RK / time_integ_RK_steady
+  MODE_SSP42 = 1,     // time_integ_SSPRK / time_integ_SSPRK_steady
+  MODE_SSP3 = 2,      // SSP-RK3 extension (Shu-Osher)
+};
+
+struct DevView {
+  int nc = 0, nint = 0, nedge = 0, nblk_red = 0;
+  // cells
+  double* U = nullptr;      // [nc] x 4 conservative state
+  double* U0 = nullptr;     // [nc] x 4 state at the start of the step
+  double* F = nullptr;      // [nc] x 4 RK accumulator (fcvar)
+  void* Pv = nullptr;       // [nc] x 4 primitives (T)
+  void* Gx = nullptr;       // [nc] x 4 d/dx primitives (T)
+  void* Gy = nullptr;       // [nc] x 4 d/dy primitives (T)
+  void* phi = nullptr;      // [nc] limiter (T)
+  double* ws = nullptr;     // [nc] sum 0.5(|un|+a)A
+  double* dtl = nullptr;    // [nc] local time step
+  double* resid = nullptr;  // [nc] x 4 residual (standalone residual only)
+  const double* vol = nullptr;
+  const double* rvol = nullptr;  // 1/vol (MIXED only)
+  const void* eps2 = nullptr;    // [nc] (T)
+  const int4* cflist = nullptr;  // [nc] signed flux slots, reference summation order
+  const void* cpos = nullptr;    // [nc][4] x 2 face-centre offsets (T) for the limiter
+  const int8_t* nvrt = nullptr;
+  const int* st_ptr = nullptr;
+  const int* st_cell = nullptr;
+  const void* st_coef = nullptr;  // LSQ/GGCB [len] x 2 (T); GGNB [len] (T)
+  const void* st_w = nullptr;     // LSQ [len] (T)
+  const int8_t* st_node = nullptr;
+  const void* coef0 = nullptr;    // [nc] x 2 (T)
+  const void* coefedg = nullptr;  // [nc][4] x 2 (T)
+  // edges
+  const int2* ecell = nullptr;    // (L,R) device cell ids; R = -1 on boundary edges
+  const void* enrm = nullptr;     // [nedge] x 2 unit normal (T)
+  const void* earea = nullptr;    // [nedge] (T)
+  const void* edL = nullptr;      // [nedge] x 2 xf - xcL (T)
+  const void* edR = nullptr;      // [nint] x 2 xf - xcR (T)
+  const int* ebtype = nullptr;    // [nedge-nint] boundary type
+  const void* exy = nullptr;      // [nedge-nint] x 2 face centre (T)
+  void* eflux = nullptr;          // [nedge] x 4 flux*area (T)
+  void* ews = nullptr;            // [nedge] ws_max*area (T)
+  // reduction and step control
+  double* partials = nullptr;     // [nblk_red] x 4
+  double* norms = nullptr;        // [norm_cap] x 4
+  int norm_cap = 0;
+  int* stepctl = nullptr;         // [0] = steps done in this call
+  double* tctl = nullptr;         // [0] = t1, [1] = told of the current step
+  // scheme
+  double gamma = 1.4, khalf = 0, nkhalf = 0, omk = 1, cfl = 1, dt = 0;
+  int limiter = 0, grad_method = 3, first_order = 0, vortex = 0;
+  double vx = 0, vy = 0, vkappa = 0, vinf[4] = {0, 0, 0, 0};
+  double pinf[4] = {0, 0, 0, 0};
+  double mc[16];
+};
+
+struct StageParams {
+  int stage = 1, nstages = 4, mode = MODE_RK, steady = 0, last = 0;
+  double h = 0;       // h_rk(stage) (unsteady)
+  double cst = 0;     // steady multiplier of dt_local
+  double coef = 1;    // rk_coef(stage)
+  double a = 0, b = 1;  // SSP3 Shu-Osher weights
+  double dts = 0;     // stage time offset from told
+};
+
+// Kernel launchers, one set per arithmetic variant (strict FP64, FP64 with
+// FMA, mixed).  All launch on the given stream; none synchronises.
+struct KernelSet {
+  const char* name;
+  void (*begin_step)(const DevView&, cudaStream_t);
+  void (*cvar2pvar)(const DevView&, cudaStream_t);
+  void (*gradient)(const DevView&, cudaStream_t);
+  void (*flux)(const DevView&, double dts, cudaStream_t);
+  void (*update)(const DevView&, const StageParams&, cudaStream_t);
+  void (*residual_out)(const DevView&, cudaStream_t);
+  void (*norm_final)(const DevView&, cudaStream_t);
+};
+const KernelSet& kernels_fp64_strict();
+const KernelSet& kernels_fp64_fast();
+const KernelSet& kernels_mixed();
+
+}  // namespace fvs

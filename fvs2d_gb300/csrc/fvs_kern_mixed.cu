@@ -1,0 +1,15 @@
+// fvs_kern_mixed.cu — device kernels, mixed precision: FP32 gradient, limiter, reconstruction and Roe flux;
+// FP64 residual accumulation, state update, local time step and norms.
+#define FVS_NS k_mixed
+#define FVS_T float
+#define FVS_MIXED 1
+#include "fvs_kernels.cuh"
+
+namespace fvs {
+const KernelSet& kernels_mixed() {
+  static const KernelSet k = {"mixed", k_mixed::launch_begin_step, k_mixed::launch_cvar2pvar, k_mixed::launch_gradient,
+                              k_mixed::launch_flux, k_mixed::launch_update, k_mixed::launch_residual_out,
+                              k_mixed::launch_norm_final};
+  return k;
+}
+}  // namespace fvs

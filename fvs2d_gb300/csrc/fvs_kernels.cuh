@@ -1,0 +1,558 @@
+// fvs_kernels.cuh — device code of the residual-and-update loop.
+//
+// Included by three translation units that differ only in arithmetic:
+//   fvs_kern_strict.cu  FP64, -fmad=false: every product and sum rounded as
+//                       the reference writes it (bit-identical to the oracle)
+//   fvs_kern_fast.cu    FP64, -fmad=true (FMA contraction allowed)
+//   fvs_kern_mixed.cu   T = float for gradient, limiter, reconstruction and
+//                       flux; FP64 residual accumulation, update and norms
+// FVS_NS names the namespace, FVS_T the compute type.
+//
+// One RK stage is three launches, all coalesced one-thread-per-item gathers:
+//   k_gradient  cell-parallel: gradient of the primitives (LSQ / GG-cell /
+//               GG-node) fused with the limiter (src/gradient_*.f90,
+//               src/gradient_limiter.f90)
+//   k_flux      edge-parallel: MUSCL reconstruction + Roe flux on interior
+//               edges, ghost state + Roe on boundary edges; writes flux*area
+//               and ws*area per edge slot (src/residual.f90:66-157,
+//               src/flux_invscid.f90:37-136)
+//   k_update    cell-parallel: sums the cell's edge slots in the reference's
+//               summation order (deterministic, no atomics), -R/vol, local
+//               time step, RK stage update, primitives for the next stage and
+//               per-block partial norms (src/runge_kutta.f90)
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "fvs_internal.hpp"
+
+namespace fvs {
+namespace FVS_NS {
+
+using T = FVS_T;
+struct T2 { T x, y; };
+
+__device__ __forceinline__ void ld4(const double* __restrict__ p, int i, double* o) {
+  const double2* q = reinterpret_cast<const double2*>(p) + 2 * (size_t)i;
+  double2 a = q[0], b = q[1];
+  o[0] = a.x; o[1] = a.y; o[2] = b.x; o[3] = b.y;
+}
+__device__ __forceinline__ void st4(double* __restrict__ p, int i, const double* v) {
+  double2* q = reinterpret_cast<double2*>(p) + 2 * (size_t)i;
+  q[0] = make_double2(v[0], v[1]);
+  q[1] = make_double2(v[2], v[3]);
+}
+__device__ __forceinline__ void ld4(const float* __restrict__ p, int i, float* o) {
+  float4 a = reinterpret_cast<const float4*>(p)[i];
+  o[0] = a.x; o[1] = a.y; o[2] = a.z; o[3] = a.w;
+}
+__device__ __forceinline__ void st4(float* __restrict__ p, int i, const float* v) {
+  reinterpret_cast<float4*>(p)[i] = make_float4(v[0], v[1], v[2], v[3]);
+}
+__device__ __forceinline__ T2 ld2(const void* p, int i) {
+  return reinterpret_cast<const T2*>(p)[i];
+}
+
+__device__ __forceinline__ double dsqrt_(double x) { return sqrt(x); }
+__device__ __forceinline__ float dsqrt_(float x) { return sqrtf(x); }
+__device__ __forceinline__ double dabs_(double x) { return fabs(x); }
+__device__ __forceinline__ float dabs_(float x) { return fabsf(x); }
+
+// limiter, src/gradient_limiter.f90:103-134 (eps2 precomputed per cell)
+__device__ __forceinline__ T limiter_fn(int type, T a, T b, T eps2) {
+  if (type == FVS_LIM_VENK) return ((a * a + eps2) + T(2) * b * a) / (a * a + T(2) * (b * b) + a * b + eps2);
+  if (type == FVS_LIM_BARTH) { T q = a / b; return q < T(1) ? q : T(1); }
+  T l = ((b * b + eps2) * a + (a * a + eps2) * b) / (a * a + b * b + T(2) * eps2);
+  return l / (b + eps2);
+}
+
+// flux_invscid_roe, src/flux_invscid.f90:37-136 (same operation order)
+__device__ __forceinline__ void roe_flux(T gamma, const T* pl, const T* pr, T nx, T ny, T* flux, T& ws_max) {
+  const T tx = -ny, ty = nx;
+  const T rhoL = pl[0], uL = pl[1], vL = pl[2], pL = pl[3];
+  const T rhoR = pr[0], uR = pr[1], vR = pr[2], pR = pr[3];
+  const T unL = uL * nx + vL * ny, unR = uR * nx + vR * ny;
+  const T utL = uL * tx + vL * ty, utR = uR * tx + vR * ty;
+  const T aL = dsqrt_(gamma * pL / rhoL), aR = dsqrt_(gamma * pR / rhoR);
+  const T kL = T(0.5) * (uL * uL + vL * vL), kR = T(0.5) * (uR * uR + vR * vR);
+  const T HL = aL * aL / (gamma - T(1)) + kL, HR = aR * aR / (gamma - T(1)) + kR;
+  const T RT = dsqrt_(rhoR / rhoL);
+  const T rho = RT * rhoL;
+  const T u = (uL + RT * uR) / (T(1) + RT);
+  const T v = (vL + RT * vR) / (T(1) + RT);
+  const T H = (HL + RT * HR) / (T(1) + RT);
+  const T a = dsqrt_((gamma - T(1)) * (H - T(0.5) * (u * u + v * v)));
+  const T un = u * nx + v * ny;
+  const T ut = u * tx + v * ty;
+  const T drho = rhoR - rhoL, dp = pR - pL, dun = unR - unL, dut = utR - utL;
+  T LdU[4], ws[4];
+  LdU[0] = (dp - rho * a * dun) / (T(2) * a * a);
+  LdU[1] = rho * dut;
+  LdU[2] = drho - dp / (a * a);
+  LdU[3] = (dp + rho * a * dun) / (T(2) * a * a);
+  ws[0] = dabs_(un - a); ws[1] = dabs_(un); ws[2] = dabs_(un); ws[3] = dabs_(un + a);
+  const T dws = T(1) / T(5);
+  if (ws[0] < dws) ws[0] = T(0.5) * (ws[0] * ws[0] / dws + dws);
+  if (ws[3] < dws) ws[3] = T(0.5) * (ws[3] * ws[3] / dws + dws);
+  const T tke = T(0.5) * (u * u + v * v);
+  const T Rv[4][4] = {{T(1), T(0), T(1), T(1)},
+                      {u - a * nx, tx, u, u + a * nx},
+                      {v - a * ny, ty, v, v + a * ny},
+                      {H - un * a, ut, tke, H + un * a}};
+  T diss[4];
+#pragma unroll
+  for (int i = 0; i < 4; i++) {
+    T s = T(0);
+#pragma unroll
+    for (int j = 0; j < 4; j++) s = s + ws[j] * LdU[j] * Rv[i][j];
+    diss[i] = s;
+  }
+  T fL[4], fR[4];
+  fL[0] = rhoL * unL;
+  fL[1] = rhoL * unL * uL + pL * nx;
+  fL[2] = rhoL * unL * vL + pL * ny;
+  fL[3] = rhoL * unL * HL;
+  fR[0] = rhoR * unR;
+  fR[1] = rhoR * unR * uR + pR * nx;
+  fR[2] = rhoR * unR * vR + pR * ny;
+  fR[3] = rhoR * unR * HR;
+#pragma unroll
+  for (int i = 0; i < 4; i++) flux[i] = T(0.5) * (fL[i] + fR[i] - T(1) * diss[i]);
+  ws_max = T(0.5) * (dabs_(un) + a);
+}
+
+// ---------------------------------------------------------------------------
+// gradient (+ limiter) : one thread per cell
+// ---------------------------------------------------------------------------
+template <int METHOD, int LIM>
+__global__ void __launch_bounds__(256) k_gradient(const DevView d) {
+  const int ic = blockIdx.x * blockDim.x + threadIdx.x;
+  if (ic >= d.nc) return;
+  const T* __restrict__ P = static_cast<const T*>(d.Pv);
+  T pc[4], gx[4], gy[4], pmin[4], pmax[4];
+  ld4(P, ic, pc);
+#pragma unroll
+  for (int v = 0; v < 4; v++) { pmin[v] = pc[v]; pmax[v] = pc[v]; }
+  const int b = d.st_ptr[ic], e = d.st_ptr[ic + 1];
+  if (METHOD == FVS_GRAD_LSQ) {
+    // grad_lsq, src/gradient_lsq.f90:393-401: sum over the stencil of
+    // (coef * (p_j - p_i)) * w, stencil outer, variable inner
+#pragma unroll
+    for (int v = 0; v < 4; v++) { gx[v] = T(0); gy[v] = T(0); }
+    const T* __restrict__ W = static_cast<const T*>(d.st_w);
+    for (int k = b; k < e; k++) {
+      const int jc = d.st_cell[k];
+      T pj[4];
+      ld4(P, jc, pj);
+      const T2 c = ld2(d.st_coef, k);
+      const T w = W[k];
+#pragma unroll
+      for (int v = 0; v < 4; v++) {
+        const T diff = pj[v] - pc[v];
+        gx[v] = gx[v] + c.x * diff * w;
+        gy[v] = gy[v] + c.y * diff * w;
+        if (LIM) {
+          pmin[v] = pj[v] < pmin[v] ? pj[v] : pmin[v];
+          pmax[v] = pj[v] > pmax[v] ? pj[v] : pmax[v];
+        }
+      }
+    }
+  } else if (METHOD == FVS_GRAD_GGCB) {
+    // grad_ggcb, src/gradient_ggcb.f90:123-135
+    const T2 c0 = ld2(d.coef0, ic);
+#pragma unroll
+    for (int v = 0; v < 4; v++) { gx[v] = c0.x * pc[v]; gy[v] = c0.y * pc[v]; }
+    for (int k = b; k < e; k++) {
+      T pj[4];
+      ld4(P, d.st_cell[k], pj);
+      const T2 c = ld2(d.st_coef, k);
+#pragma unroll
+      for (int v = 0; v < 4; v++) { gx[v] = gx[v] + c.x * pj[v]; gy[v] = gy[v] + c.y * pj[v]; }
+    }
+    const T vol = T(d.vol[ic]);
+#pragma unroll
+    for (int v = 0; v < 4; v++) { gx[v] = gx[v] / vol; gy[v] = gy[v] / vol; }
+  } else {
+    // grad_ggnb, src/gradient_ggnb.f90:190-207
+    const T2 c0 = ld2(d.coef0, ic);
+#pragma unroll
+    for (int v = 0; v < 4; v++) { gx[v] = c0.x * pc[v]; gy[v] = c0.y * pc[v]; }
+    const T* __restrict__ CN = static_cast<const T*>(d.st_coef);
+    for (int k = b; k < e; k++) {
+      T pj[4];
+      ld4(P, d.st_cell[k], pj);
+      const T cn = CN[k];
+      const T2 ce = ld2(d.coefedg, 4 * ic + d.st_node[k]);
+#pragma unroll
+      for (int v = 0; v < 4; v++) { gx[v] = gx[v] + ce.x * cn * pj[v]; gy[v] = gy[v] + ce.y * cn * pj[v]; }
+    }
+    const T vol = T(d.vol[ic]);
+#pragma unroll
+    for (int v = 0; v < 4; v++) { gx[v] = gx[v] / vol; gy[v] = gy[v] / vol; }
+  }
+  st4(static_cast<T*>(d.Gx), ic, gx);
+  st4(static_cast<T*>(d.Gy), ic, gy);
+  if (LIM) {
+    // compute_gradient_limiter, src/gradient_limiter.f90:47-88
+    const int nv = d.nvrt[ic];
+    const T eps2 = static_cast<const T*>(d.eps2)[ic];
+    T2 cp[4];
+#pragma unroll
+    for (int f = 0; f < 4; f++) cp[f] = ld2(d.cpos, 4 * ic + f);
+    T phimin = T(1);
+#pragma unroll
+    for (int v = 0; v < 4; v++) {
+      T pe[4] = {T(100), T(100), T(100), T(100)};
+#pragma unroll
+      for (int f = 0; f < 4; f++) {
+        if (f >= nv) break;
+        const T pf = pc[v] + cp[f].x * gx[v] + cp[f].y * gy[v];
+        const T dmax = pmax[v] - pc[v], dmin = pmin[v] - pc[v], diff = pf - pc[v];
+        if (diff > T(0)) pe[f] = limiter_fn(d.limiter, dmax, diff, eps2);
+        else if (diff < T(0)) pe[f] = limiter_fn(d.limiter, dmin, diff, eps2);
+        else pe[f] = T(1);
+      }
+      T mv = pe[0];
+#pragma unroll
+      for (int f = 1; f < 4; f++) mv = pe[f] < mv ? pe[f] : mv;
+      const T ph = mv < T(1) ? mv : T(1);
+      phimin = (v == 0 || ph < phimin) ? ph : phimin;
+    }
+    static_cast<T*>(d.phi)[ic] = phimin;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// boundary ghost state, bc_flux src/residual.f90:183-255
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double texp_(double x) { return exp(x); }
+__device__ __forceinline__ float texp_(float x) { return expf(x); }
+__device__ __forceinline__ double tpow_(double x, double y) { return pow(x, y); }
+__device__ __forceinline__ float tpow_(float x, float y) { return powf(x, y); }
+__device__ __forceinline__ double tsin_(double x) { return sin(x); }
+__device__ __forceinline__ float tsin_(float x) { return sinf(x); }
+__device__ __forceinline__ double tcos_(double x) { return cos(x); }
+__device__ __forceinline__ float tcos_(float x) { return cosf(x); }
+
+__device__ __forceinline__ void ghost_state(const DevView& d, int type, double time, T x, T y, T nx, T ny,
+                                            const T* pfL, T* pfR) {
+  if (type == FVS_BC_FREESTREAM) {
+#pragma unroll
+    for (int k = 0; k < 4; k++) pfR[k] = T(d.pinf[k]);
+  } else if (type == FVS_BC_SLIP_WALL) {
+    const T un = pfL[1] * nx + pfL[2] * ny;
+    pfR[0] = pfL[0];
+    pfR[1] = pfL[1] - T(2) * un * nx;
+    pfR[2] = pfL[2] - T(2) * un * ny;
+    pfR[3] = pfL[3];
+  } else if (d.vortex) {
+    // compute_isentropic_vortex, src/mms.f90:219-265
+    const T g = T(d.gamma), q = T(d.vkappa) / (T(2) * T(3.141592653589793238462643383279502884));
+    const T T_inf = T(d.vinf[3]) / T(d.vinf[0]);
+    const T dx = x - (T(d.vx) + T(d.vinf[1]) * T(time));
+    const T dy = y - (T(d.vy) + T(d.vinf[2]) * T(time));
+    const T r = dsqrt_(dx * dx + dy * dy);
+    pfR[1] = T(d.vinf[1]) - q * dy * texp_(T(0.5) * (T(1) - r * r));
+    pfR[2] = T(d.vinf[2]) + q * dx * texp_(T(0.5) * (T(1) - r * r));
+    const T temp = T_inf - (q * q) * (g - T(1)) / (T(2) * g) * texp_(T(1) - r * r);
+    pfR[0] = tpow_(temp, T(1) / (g - T(1)));
+    pfR[3] = tpow_(pfR[0], g);
+  } else {
+    // manufactured solution, src/mms.f90:187-213 (values only)
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      const double* m = d.mc + 4 * k;
+      pfR[k] = T(m[0]) + T(m[1]) * tsin_(T(m[2]) * x + T(m[3]) * y);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// edge fluxes : one thread per edge slot
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_flux(const DevView d, double dts) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= d.nedge) return;
+  const T* __restrict__ P = static_cast<const T*>(d.Pv);
+  const T* __restrict__ GX = static_cast<const T*>(d.Gx);
+  const T* __restrict__ GY = static_cast<const T*>(d.Gy);
+  const T* __restrict__ PH = static_cast<const T*>(d.phi);
+  const int2 lr = d.ecell[e];
+  const T2 n = ld2(d.enrm, e);
+  const T af = static_cast<const T*>(d.earea)[e];
+  const T2 dl = ld2(d.edL, e);
+  T pl[4], gxl[4], gyl[4], pfL[4], pfR[4];
+  ld4(P, lr.x, pl);
+  ld4(GX, lr.x, gxl);
+  ld4(GY, lr.x, gyl);
+  const T phiL = PH[lr.x];
+  if (e < d.nint) {
+    // src/residual.f90:83-92
+    T pr[4], gxr[4], gyr[4];
+    ld4(P, lr.y, pr);
+    ld4(GX, lr.y, gxr);
+    ld4(GY, lr.y, gyr);
+    const T phiR = PH[lr.y];
+    const T2 dr = ld2(d.edR, e);
+    const T kh = T(d.khalf), nkh = T(d.nkhalf), omk = T(d.omk);
+#pragma unroll
+    for (int v = 0; v < 4; v++) {
+      const T gradC = pr[v] - pl[v];
+      const T gradL = dl.x * gxl[v] + dl.y * gyl[v];
+      const T gradR = dr.x * gxr[v] + dr.y * gyr[v];
+      pfL[v] = pl[v] + phiL * (kh * gradC + omk * gradL);
+      pfR[v] = pr[v] + phiR * (nkh * gradC + omk * gradR);
+    }
+  } else {
+    // src/residual.f90:128-137
+#pragma unroll
+    for (int v = 0; v < 4; v++) pfL[v] = pl[v] + phiL * (dl.x * gxl[v] + dl.y * gyl[v]);
+    const int bi = e - d.nint;
+    const T2 xy = ld2(d.exy, bi);
+    ghost_state(d, d.ebtype[bi], d.tctl[1] + dts, xy.x, xy.y, n.x, n.y, pfL, pfR);
+  }
+  T flux[4], wsm;
+  roe_flux(T(d.gamma), pfL, pfR, n.x, n.y, flux, wsm);
+#pragma unroll
+  for (int v = 0; v < 4; v++) flux[v] = flux[v] * af;
+  st4(static_cast<T*>(d.eflux), e, flux);
+  static_cast<T*>(d.ews)[e] = wsm * af;
+}
+
+// ---------------------------------------------------------------------------
+// per-cell gather of the edge slots in the reference's summation order
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void gather_slot(const DevView& d, int s, double* r, double& ws) {
+  if (s == 0) return;
+  const int idx = (s > 0 ? s : -s) - 1;
+  T f[4];
+  ld4(static_cast<const T*>(d.eflux), idx, f);
+  if (s > 0) {
+#pragma unroll
+    for (int v = 0; v < 4; v++) r[v] = r[v] + double(f[v]);
+  } else {
+#pragma unroll
+    for (int v = 0; v < 4; v++) r[v] = r[v] - double(f[v]);
+  }
+  ws = ws + double(static_cast<const T*>(d.ews)[idx]);
+}
+
+__device__ __forceinline__ void cell_residual(const DevView& d, int ic, double* res, double& ws) {
+  double r[4] = {0.0, 0.0, 0.0, 0.0};
+  ws = 0.0;
+  const int4 cf = d.cflist[ic];
+  gather_slot(d, cf.x, r, ws);
+  gather_slot(d, cf.y, r, ws);
+  gather_slot(d, cf.z, r, ws);
+  gather_slot(d, cf.w, r, ws);
+#if FVS_MIXED
+  const double rv = d.rvol[ic];
+#pragma unroll
+  for (int v = 0; v < 4; v++) res[v] = -r[v] * rv;
+#else
+  const double vol = d.vol[ic];
+#pragma unroll
+  for (int v = 0; v < 4; v++) res[v] = -r[v] / vol;  // src/residual.f90:164-166
+#endif
+}
+
+__device__ __forceinline__ void cons2prim(double g, const double* u, T* p) {
+#if FVS_MIXED
+  const float r = float(u[0]);
+  p[0] = r;
+  p[1] = float(u[1]) / r;
+  p[2] = float(u[2]) / r;
+  p[3] = float(g - 1.0) * (float(u[3]) - 0.5f * r * (p[1] * p[1] + p[2] * p[2]));
+#else
+  // cvar2pvar, src/data_solution.f90:78-84
+  p[0] = u[0];
+  p[1] = u[1] / u[0];
+  p[2] = u[2] / u[0];
+  p[3] = (g - 1.0) * (u[3] - 0.5 * p[0] * (p[1] * p[1] + p[2] * p[2]));
+#endif
+}
+
+// deterministic block sum of 4 doubles; thread 0 of each block writes out
+__device__ __forceinline__ void block_sum4(double* v, double* out) {
+  __shared__ double sh[8][4];
+#pragma unroll
+  for (int k = 0; k < 4; k++)
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_down_sync(0xffffffffu, v[k], o);
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0)
+#pragma unroll
+    for (int k = 0; k < 4; k++) sh[w][k] = v[k];
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const int nw = blockDim.x >> 5;
+    for (int k = 0; k < 4; k++) {
+      double s = 0.0;
+      for (int i = 0; i < nw; i++) s += sh[i][k];
+      out[k] = s;
+    }
+  }
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(256) k_update(const DevView d, const StageParams sp) {
+  const int ic = blockIdx.x * blockDim.x + threadIdx.x;
+  double d2[4] = {0.0, 0.0, 0.0, 0.0};
+  if (ic < d.nc) {
+    double res[4], ws;
+    cell_residual(d, ic, res, ws);
+    double h = sp.h;
+    if (sp.steady) {
+      double dtl;
+      if (sp.stage == 1) {  // compute_local_time, src/runge_kutta.f90:424-437
+        dtl = d.cfl * d.vol[ic] / (0.5 * ws);
+        d.dtl[ic] = dtl;
+      } else {
+        dtl = d.dtl[ic];
+      }
+      h = dtl * sp.cst;
+    }
+    double u0[4], u[4], f[4];
+    if (sp.stage == 1) {
+      ld4(d.U, ic, u0);
+      st4(d.U0, ic, u0);
+#pragma unroll
+      for (int v = 0; v < 4; v++) f[v] = 0.0;
+    } else {
+      ld4(d.U0, ic, u0);
+      if (MODE != MODE_SSP3) ld4(d.F, ic, f);
+    }
+    if (MODE == MODE_SSP42) {
+      // src/runge_kutta.f90:225-226 / :383-387
+#pragma unroll
+      for (int v = 0; v < 4; v++) {
+        u[v] = u0[v] + h * (sp.coef * res[v] + f[v]);
+        f[v] = f[v] + res[v];
+      }
+      if (!sp.last) st4(d.F, ic, f);
+    } else if (MODE == MODE_RK) {
+      // src/runge_kutta.f90:156-162 / :302-313
+#pragma unroll
+      for (int v = 0; v < 4; v++) {
+        f[v] = f[v] + sp.coef * res[v];
+        u[v] = sp.last ? u0[v] + h * f[v] : u0[v] + h * res[v];
+      }
+      if (!sp.last) st4(d.F, ic, f);
+    } else {
+      // SSP-RK3 (Shu-Osher), extension
+      double cur[4];
+      if (sp.stage == 1) {
+#pragma unroll
+        for (int v = 0; v < 4; v++) cur[v] = u0[v];
+      } else {
+        ld4(d.U, ic, cur);
+      }
+#pragma unroll
+      for (int v = 0; v < 4; v++) {
+        const double s = cur[v] + h * res[v];
+        u[v] = sp.stage == 1 ? s : sp.a * u0[v] + sp.b * s;
+      }
+    }
+    st4(d.U, ic, u);
+    T p[4];
+    cons2prim(d.gamma, u, p);
+    st4(static_cast<T*>(d.Pv), ic, p);
+    if (sp.last) {
+#pragma unroll
+      for (int v = 0; v < 4; v++) {
+        const double dd = fabs(u[v] - u0[v]);
+        d2[v] = dd * dd;
+      }
+    }
+  }
+  if (sp.last) {
+    double out[4];
+    block_sum4(d2, out);
+    if (threadIdx.x == 0)
+#pragma unroll
+      for (int k = 0; k < 4; k++) d.partials[4 * blockIdx.x + k] = out[k];
+  }
+}
+
+// standalone compute_residual output: resid and ws_nrml
+__global__ void __launch_bounds__(256) k_residual_out(const DevView d) {
+  const int ic = blockIdx.x * blockDim.x + threadIdx.x;
+  if (ic >= d.nc) return;
+  double res[4], ws;
+  cell_residual(d, ic, res, ws);
+  st4(d.resid, ic, res);
+  d.ws[ic] = ws;
+}
+
+__global__ void __launch_bounds__(256) k_cvar2pvar(const DevView d) {
+  const int ic = blockIdx.x * blockDim.x + threadIdx.x;
+  if (ic >= d.nc) return;
+  double u[4];
+  T p[4];
+  ld4(d.U, ic, u);
+  cons2prim(d.gamma, u, p);
+  st4(static_cast<T*>(d.Pv), ic, p);
+}
+
+// told = t1 + (istep-1)*dt, src/runge_kutta.f90:207-208
+__global__ void k_begin_step(const DevView d) {
+  const int istep = d.stepctl[0] + 1;
+  d.tctl[1] = d.tctl[0] + double(istep - 1) * d.dt;
+}
+
+// RMS of |U - U0| per component from the block partials: one block,
+// fixed-order sums (deterministic)
+__global__ void __launch_bounds__(256) k_norm_final(const DevView d) {
+  double s[4] = {0.0, 0.0, 0.0, 0.0};
+  for (int i = threadIdx.x; i < d.nblk_red; i += blockDim.x)
+#pragma unroll
+    for (int k = 0; k < 4; k++) s[k] += d.partials[4 * i + k];
+  double out[4];
+  block_sum4(s, out);
+  if (threadIdx.x == 0) {
+    const int istep = d.stepctl[0] + 1;
+    double* o = d.norms + 4 * (size_t)((istep - 1) % d.norm_cap);
+#pragma unroll
+    for (int k = 0; k < 4; k++) o[k] = sqrt(out[k] / double(d.nc));
+    d.stepctl[0] = istep;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// launchers
+// ---------------------------------------------------------------------------
+static inline unsigned grid_of(int n) { return (unsigned)((n + 255) / 256); }
+
+static void launch_begin_step(const DevView& d, cudaStream_t s) { k_begin_step<<<1, 1, 0, s>>>(d); }
+static void launch_cvar2pvar(const DevView& d, cudaStream_t s) { k_cvar2pvar<<<grid_of(d.nc), 256, 0, s>>>(d); }
+
+static void launch_gradient(const DevView& d, cudaStream_t s) {
+  if (d.first_order) return;
+  const unsigned g = grid_of(d.nc);
+  const bool lim = d.limiter != FVS_LIM_NONE;
+  switch (d.grad_method) {
+    case FVS_GRAD_LSQ:
+      if (lim) k_gradient<FVS_GRAD_LSQ, 1><<<g, 256, 0, s>>>(d);
+      else k_gradient<FVS_GRAD_LSQ, 0><<<g, 256, 0, s>>>(d);
+      break;
+    case FVS_GRAD_GGCB: k_gradient<FVS_GRAD_GGCB, 0><<<g, 256, 0, s>>>(d); break;
+    default: k_gradient<FVS_GRAD_GGNB, 0><<<g, 256, 0, s>>>(d); break;
+  }
+}
+
+static void launch_flux(const DevView& d, double dts, cudaStream_t s) { k_flux<<<grid_of(d.nedge), 256, 0, s>>>(d, dts); }
+
+static void launch_update(const DevView& d, const StageParams& sp, cudaStream_t s) {
+  const unsigned g = grid_of(d.nc);
+  switch (sp.mode) {
+    case MODE_SSP42: k_update<MODE_SSP42><<<g, 256, 0, s>>>(d, sp); break;
+    case MODE_SSP3: k_update<MODE_SSP3><<<g, 256, 0, s>>>(d, sp); break;
+    default: k_update<MODE_RK><<<g, 256, 0, s>>>(d, sp); break;
+  }
+}
+
+static void launch_residual_out(const DevView& d, cudaStream_t s) { k_residual_out<<<grid_of(d.nc), 256, 0, s>>>(d); }
+static void launch_norm_final(const DevView& d, cudaStream_t s) { k_norm_final<<<1, 256, 0, s>>>(d); }
+
+}  // namespace FVS_NS
+}  // namespace fvs

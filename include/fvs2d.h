@@ -1,0 +1,214 @@
+/*
+ * fvs2d.h — C-ABI of the GB300 residual-and-update library for fvs2d.
+ *
+ * The reference has no FFI: its hot path is a pair of Fortran module
+ * procedures over module-global state,
+ *   compute_residual(time)            src/residual.f90:23
+ *   time_integration(t1, ntimes_sub)  src/runge_kutta.f90:94
+ * reading the mesh of src/data_grid.f90:23-68, the solution arrays of
+ * src/data_solution.f90:16-28 and the scheme flags of src/input.f90:9-56.
+ * The entry points below replace those procedures one-for-one.  A Fortran
+ * host binds them through ISO_C_BINDING (interface block in INTEGRATION.md).
+ *
+ * Conventions
+ *  - All arrays are caller-owned host memory unless a name says "device".
+ *    The library copies in and out; no pointer is kept after a call returns.
+ *  - Cell, node and edge numbers crossing the ABI are 1-based, in the
+ *    reference's numbering (cells: triangles first, then quads, as read
+ *    from the .grid file, src/grid_procs.f90:95-108).
+ *  - Per-cell 4-vectors are laid out [ncells][4] (row-major C), which is the
+ *    Fortran column-major cvar(4,ncells) of src/data_solution.f90:18.
+ *  - Every call returns an FVS_* status; nothing calls exit/stop/abort
+ *    (the reference stops the program, e.g. src/residual.f90:208,220).
+ *  - One handle is not re-entrant; separate handles may be used from
+ *    separate host threads.  Each handle owns one CUDA stream.
+ */
+#ifndef FVS2D_H
+#define FVS2D_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define FVS_OK            0
+#define FVS_ERR_INVALID   1  /* bad argument or unsupported option combination */
+#define FVS_ERR_MESH      2  /* mesh fails a reference consistency check        */
+#define FVS_ERR_CUDA      3  /* CUDA runtime error (message via fvs_last_error)  */
+#define FVS_ERR_NONFINITE 4  /* a residual norm became NaN/Inf                   */
+#define FVS_ERR_DIVERGED  5  /* residual norm grew past options.diverge_factor   */
+#define FVS_ERR_TIMEOUT   6  /* a bounded device-side wait expired               */
+#define FVS_ERR_NOMEM     7  /* device or host allocation failed                 */
+
+/* ---- boundary types (src/residual.f90:194-221; .bc strings) ------------ */
+#define FVS_BC_FREESTREAM 1  /* 'freestream'  */
+#define FVS_BC_SLIP_WALL  2  /* 'slip_wall'   */
+#define FVS_BC_SOLID_WALL 3  /* 'solid_wall'  (the reference stops: rejected) */
+#define FVS_BC_DIRICHLET  4  /* 'dirichlet'   (exact vortex or MMS)           */
+
+/* ---- gradient / limiter / reconstruction codes (src/input.f90:190-263) -- */
+#define FVS_GRAD_GGCB 1
+#define FVS_GRAD_GGNB 2
+#define FVS_GRAD_LSQ  3
+#define FVS_LSQ_FN 0          /* face-neighbour stencil, kd-tree padding  */
+#define FVS_LSQ_NN 1          /* node-neighbour stencil                    */
+#define FVS_LIM_NONE   0
+#define FVS_LIM_VENK   1
+#define FVS_LIM_BARTH  2
+#define FVS_LIM_ALBADA 3
+#define FVS_RECON_UPWIND1 1
+#define FVS_RECON_UPWIND2 2
+#define FVS_RECON_UMUSCL  3
+
+/* ---- arithmetic of the device path ---------------------------------------
+ * FP64_STRICT: every operation of the reference in source order, no FMA
+ *              contraction; bit-identical to the CPU oracle built with
+ *              -ffp-contract=off wherever no transcendental is involved.
+ * FP64:        same operations, FMA contraction allowed (fast FP64 drop-in).
+ * MIXED:       gradients, limiter, reconstruction and flux in FP32; residual
+ *              accumulation, state update, LSQ setup and norms in FP64.      */
+#define FVS_PREC_FP64_STRICT 0
+#define FVS_PREC_FP64        1
+#define FVS_PREC_MIXED       2
+
+/* ---- mesh: what grid_read / grid_bc_read load (src/grid_procs.f90:65-164) */
+typedef struct fvs_mesh {
+  int32_t nnodes;
+  int32_t ncells_tri;
+  int32_t ncells_quad;
+  const double*  node_xy;      /* [nnodes][2]                                   */
+  const int32_t* tri_nodes;    /* [ncells_tri][3], 1-based node ids             */
+  const int32_t* quad_nodes;   /* [ncells_quad][4], 1-based (may be NULL if 0)  */
+  int32_t nbndries;
+  const int32_t* bndry_ncells; /* [nbndries]                                    */
+  const int32_t* bndry_type;   /* [nbndries] FVS_BC_*                           */
+  const int32_t* bndry_cells;  /* concatenated per boundary, 1-based cell ids   */
+  /* Extension, not in the reference: doubly periodic meshes.  When > 0 the
+   * node ids of cells wrap across x (resp. y) with this period and every
+   * geometric difference is taken as the minimum image.                    */
+  double period_x;
+  double period_y;
+} fvs_mesh;
+
+/* ---- options: the scheme flags of src/input.f90:9-56 ------------------- */
+typedef struct fvs_options {
+  double  gamma;        /* gamma (cp/cv)                                      */
+  double  mach_inf;     /* free-stream Mach (src/data_solution.f90:55-58)     */
+  double  aoa_inf_deg;  /* free-stream angle of attack, degrees               */
+  double  dt;           /* time step (unsteady); initial dt_local (steady)    */
+  double  cfl;          /* cfl_user (steady local time step)                  */
+  int32_t steady;       /* lsteady: local time stepping                       */
+  int32_t vortex;       /* lvortex: Dirichlet BC = exact isentropic vortex    */
+  int32_t ntstart;      /* 0 -> manufactured solution (MMS) start and BC      */
+  int32_t grad_method;  /* FVS_GRAD_*                                         */
+  int32_t lsq_stencil;  /* FVS_LSQ_FN / FVS_LSQ_NN                            */
+  double  lsq_pow;      /* LSQ weight 1/d^p                                   */
+  int32_t limiter;      /* FVS_LIM_*                                          */
+  int32_t reconst;      /* FVS_RECON_*                                        */
+  double  umuscl;       /* kappa (forced 0 for methods 1-2)                   */
+  int32_t flux;         /* 1 = Roe (the only scheme)                          */
+  int32_t rk_nstages;   /* 4 (reference); 3 with ssprk = SSP-RK3 (extension)  */
+  int32_t rk_order;     /* 1..4                                               */
+  int32_t ssprk;        /* lSSPRK                                             */
+  /* fvs2d.vortex (src/mms.f90:55-62) */
+  double  vortex_x, vortex_y, vortex_kappa;
+  double  vortex_inf[4];  /* rho, u, v, p */
+  /* extensions, not in the reference */
+  int32_t dt_from_cfl;  /* unsteady: dt = min_cells cfl*vol/(0.5*ws) of the  */
+                        /* first residual evaluation, kept for the whole run  */
+  int32_t precision;    /* FVS_PREC_*                                         */
+  double  diverge_factor; /* >0: FVS_ERR_DIVERGED when rho-norm > factor*first */
+} fvs_options;
+
+typedef struct fvs_handle fvs_handle;
+
+/* Fills the defaults of the reference's example inputs (LSQ-fn, p=0, no
+ * limiter, 2nd-order upwind, Roe, classic RK4, gamma 1.4). */
+int fvs_options_default(fvs_options* opt);
+
+/* Builds connectivity bit-exactly as grid_data (src/grid_procs.f90:170-794),
+ * the gradient operator (src/gradient.f90:18-38 and the grad_*_init
+ * routines), verifies LSQ linear exactness (src/gradient_lsq.f90:490-529),
+ * sets the free-stream state (src/data_solution.f90:41-66) and the RK
+ * coefficients (src/runge_kutta.f90:25-88), renumbers cells for the device
+ * and uploads everything.  On failure *out is NULL and the message is
+ * available from fvs_last_error(NULL). */
+int fvs_create(const fvs_mesh* mesh, const fvs_options* opt, fvs_handle** out);
+/* Host-only handle: runs the mesh preprocessing and the gradient setup of
+ * fvs_create without touching a GPU (for hosts that only need the
+ * reference-numbered connectivity, or machines without a device).  Only
+ * fvs_get_sizes, fvs_export*, fvs_mms_source and fvs_destroy accept it. */
+int fvs_create_host(const fvs_mesh* mesh, const fvs_options* opt, fvs_handle** out);
+void fvs_destroy(fvs_handle* h);
+/* Last error message of h, or of the calling thread's last failed create
+ * when h is NULL.  The string lives until the next call on that handle. */
+const char* fvs_last_error(const fvs_handle* h);
+
+typedef struct fvs_sizes {
+  int32_t nnodes, ncells, ncells_tri, ncells_quad;
+  int32_t nedges, nedges_intr, nedges_bndr;
+  int32_t ncells_intr, ncells_bndr;
+  int32_t nbndries;
+  int32_t stencil_len;   /* total entries of the gradient stencil CSR       */
+  int32_t nstages;       /* RK stages per step                              */
+  double  heff1, heff2;  /* src/grid_procs.f90:233-243                      */
+  double  vol_sum, vol_green; /* grid_data_verify src/grid_procs.f90:824-840 */
+  double  dt;            /* current global dt                               */
+} fvs_sizes;
+int fvs_get_sizes(const fvs_handle* h, fvs_sizes* s);
+
+/* Named host-side setup arrays in reference order (connectivity, geometry,
+ * stencils), for bit-level comparison: see fvs_export for the names. */
+int fvs_export_size(const fvs_handle* h, const char* name, int64_t* nbytes);
+int fvs_export(const fvs_handle* h, const char* name, void* dst, int64_t nbytes);
+
+/* initialize_solution (src/initialize.f90:19-90) for ntstart <= 1:
+ * free stream, exact vortex at t=(ntstart-1)*dt, or MMS. */
+int fvs_init_state(fvs_handle* h);
+int fvs_set_state(fvs_handle* h, const double* cvar);   /* [ncells][4] */
+int fvs_get_state(fvs_handle* h, double* cvar);         /* [ncells][4] */
+
+/* compute_residual (src/residual.f90:23-177): resid = dU/dt = -R/vol and
+ * ws_nrml = sum of 0.5(|un|+a)*A.  Either output may be NULL. */
+int fvs_residual(fvs_handle* h, double time, double* resid, double* ws_nrml);
+/* Gradient grad(4,ncells,2) as [2][ncells][4] and phi_lim[ncells] of the
+ * last residual evaluation (src/data_solution.f90:19-21). */
+int fvs_get_gradient(fvs_handle* h, double* grad, double* phi);
+
+/* time_integration (src/runge_kutta.f90:94-114): nsteps RK steps from t1.
+ * resnorm (may be NULL) receives [nsteps][4] RMS(|U-U0|) per component,
+ * the log_res.plt columns (src/runge_kutta.f90:395-410). */
+int fvs_time_integration(fvs_handle* h, double t1, int32_t nsteps, double* resnorm);
+
+/* Extension: steps until RMS(dU_rho)(n) <= drop * RMS(dU_rho)(1) or
+ * max_steps.  The norm is checked on the host every check_every steps
+ * (steps run as captured CUDA graphs in between). */
+int fvs_run_to_drop(fvs_handle* h, double t1, int32_t max_steps, double drop,
+                    int32_t check_every, int32_t* steps_done, double* resnorm);
+
+/* error_isentropic_vortex (src/mms.f90:271-365): the 13 numbers of one
+ * log_vortex_err.plt row after the time column. */
+int fvs_vortex_error(fvs_handle* h, double time, double* err13);
+
+/* MMS source term at cell centres (src/mms.f90:105-114), [ncells][4]. */
+int fvs_mms_source(fvs_handle* h, double* src);
+
+/* ---- device-resident path (benchmarks, batched drivers) --------------- */
+/* Runs nsteps steps on the device state without host copies; if ms is not
+ * NULL it receives the CUDA-event time of the call on the handle's stream. */
+int fvs_steps_device(fvs_handle* h, int32_t nsteps, float* ms);
+/* Per-kernel timing of one step (CUDA events on the handle's stream):
+ * names[i] / ms[i] for up to cap kernels; returns the count in *n. */
+int fvs_profile_step(fvs_handle* h, int32_t cap, int32_t* n, char* names /*[cap][32]*/, float* ms);
+/* Number of kernel launches one step issues. */
+int fvs_launches_per_step(const fvs_handle* h, int32_t* n);
+/* Device pointer of the conservative state (RCM order) and the permutation
+ * old->new (host copy, 0-based) for callers that keep data on the device. */
+int fvs_device_state(fvs_handle* h, void** dptr);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FVS2D_H */
