@@ -272,6 +272,7 @@ int build_device(fvs_handle* H) {
   std::vector<T> st_coef, st_w, coef0, coefedg;
   std::vector<int8_t> st_node;
   const bool ggnb = h.grad_method == FVS_GRAD_GGNB;
+  const bool fold_w = h.grad_method == FVS_GRAD_LSQ && H->o.precision != FVS_PREC_FP64_STRICT;
   for (int dc = 0; dc < nc; dc++) {
     int o = iperm[dc];
     for (int k = h.st_ptr[o]; k < h.st_ptr[o + 1]; k++) {
@@ -279,6 +280,10 @@ int build_device(fvs_handle* H) {
       if (ggnb) {
         st_coef.push_back(T(h.st_coef[k]));
         st_node.push_back(h.st_node[k]);
+      } else if (fold_w) {
+        // FP64 / MIXED: the LSQ weight folded into the coefficients (setup in FP64)
+        st_coef.push_back(T(h.st_coef[2 * k] * h.st_w[k]));
+        st_coef.push_back(T(h.st_coef[2 * k + 1] * h.st_w[k]));
       } else {
         st_coef.push_back(T(h.st_coef[2 * k]));
         st_coef.push_back(T(h.st_coef[2 * k + 1]));

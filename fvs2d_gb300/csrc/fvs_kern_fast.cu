@@ -2,6 +2,7 @@
 #define FVS_NS k_fast
 #define FVS_T double
 #define FVS_MIXED 0
+#define FVS_STRICT 0
 #include "fvs_kernels.cuh"
 
 namespace fvs {

@@ -3,6 +3,7 @@
 #define FVS_NS k_mixed
 #define FVS_T float
 #define FVS_MIXED 1
+#define FVS_STRICT 0
 #include "fvs_kernels.cuh"
 
 namespace fvs {

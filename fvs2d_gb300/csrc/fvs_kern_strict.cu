@@ -3,6 +3,7 @@
 #define FVS_NS k_strict
 #define FVS_T double
 #define FVS_MIXED 0
+#define FVS_STRICT 1
 #include "fvs_kernels.cuh"
 
 namespace fvs {

@@ -121,6 +121,59 @@ __device__ __forceinline__ void roe_flux(T gamma, const T* pl, const T* pr, T nx
   ws_max = T(0.5) * (dabs_(un) + a);
 }
 
+// The same Roe flux, algebraically rearranged for fewer FP64 instructions
+// (FP64 and MIXED builds; the strict build keeps the source form above):
+//  - aL, aR enter only through aL*aL/(gamma-1) in HL, HR: no square roots
+//  - one reciprocal each for rhoL, rhoR, 1+RT and a*a replaces 8 divisions
+//  - the eigenvector sum drops the products with the constants 0 and 1
+// Differences to the source form are rounding-level (relative ~1e-16 per
+// operation), checked against the oracle at 1e-12.
+__device__ __forceinline__ void roe_flux_fast(T gamma, T gm1, T igm1, const T* pl, const T* pr, T nx, T ny, T* flux,
+                                              T& ws_max) {
+  const T tx = -ny, ty = nx;
+  const T rhoL = pl[0], uL = pl[1], vL = pl[2], pL = pl[3];
+  const T rhoR = pr[0], uR = pr[1], vR = pr[2], pR = pr[3];
+  const T riL = T(1) / rhoL, riR = T(1) / rhoR;
+  const T unL = uL * nx + vL * ny, unR = uR * nx + vR * ny;
+  const T utL = uL * tx + vL * ty, utR = uR * tx + vR * ty;
+  const T HL = gamma * pL * riL * igm1 + T(0.5) * (uL * uL + vL * vL);
+  const T HR = gamma * pR * riR * igm1 + T(0.5) * (uR * uR + vR * vR);
+  const T RT = dsqrt_(rhoR * riL);
+  const T rho = RT * rhoL;
+  const T i1 = T(1) / (T(1) + RT);
+  const T u = (uL + RT * uR) * i1;
+  const T v = (vL + RT * vR) * i1;
+  const T H = (HL + RT * HR) * i1;
+  const T q2 = T(0.5) * (u * u + v * v);
+  const T a2 = gm1 * (H - q2);
+  const T a = dsqrt_(a2);
+  const T ia2 = T(1) / a2;
+  const T un = u * nx + v * ny;
+  const T ut = u * tx + v * ty;
+  const T drho = rhoR - rhoL, dp = pR - pL, dun = unR - unL, dut = utR - utL;
+  const T rad = rho * a * dun;
+  const T L0 = (dp - rad) * T(0.5) * ia2;
+  const T L1 = rho * dut;
+  const T L2 = drho - dp * ia2;
+  const T L3 = (dp + rad) * T(0.5) * ia2;
+  T ws0 = dabs_(un - a), ws3 = dabs_(un + a);
+  const T ws1 = dabs_(un);
+  if (ws0 < T(0.2)) ws0 = T(0.5) * (ws0 * ws0 * T(5) + T(0.2));
+  if (ws3 < T(0.2)) ws3 = T(0.5) * (ws3 * ws3 * T(5) + T(0.2));
+  const T w0 = ws0 * L0, w1 = ws1 * L1, w2 = ws1 * L2, w3 = ws3 * L3;
+  const T s03 = w0 + w3, s = s03 + w2, dw = (w3 - w0) * a;
+  const T diss0 = s;
+  const T diss1 = u * s + dw * nx + w1 * tx;
+  const T diss2 = v * s + dw * ny + w1 * ty;
+  const T diss3 = H * s03 + un * dw + w1 * ut + w2 * q2;
+  const T mL = rhoL * unL, mR = rhoR * unR;
+  flux[0] = T(0.5) * (mL + mR - diss0);
+  flux[1] = T(0.5) * (mL * uL + mR * uR + (pL + pR) * nx - diss1);
+  flux[2] = T(0.5) * (mL * vL + mR * vR + (pL + pR) * ny - diss2);
+  flux[3] = T(0.5) * (mL * HL + mR * HR - diss3);
+  ws_max = T(0.5) * (ws1 + a);
+}
+
 // ---------------------------------------------------------------------------
 // gradient (+ limiter) : one thread per cell
 // ---------------------------------------------------------------------------
@@ -139,18 +192,28 @@ __global__ void __launch_bounds__(256) k_gradient(const DevView d) {
     // (coef * (p_j - p_i)) * w, stencil outer, variable inner
 #pragma unroll
     for (int v = 0; v < 4; v++) { gx[v] = T(0); gy[v] = T(0); }
+#if FVS_STRICT
     const T* __restrict__ W = static_cast<const T*>(d.st_w);
+#endif
     for (int k = b; k < e; k++) {
       const int jc = d.st_cell[k];
       T pj[4];
       ld4(P, jc, pj);
       const T2 c = ld2(d.st_coef, k);
+#if FVS_STRICT
       const T w = W[k];
+#endif
 #pragma unroll
       for (int v = 0; v < 4; v++) {
         const T diff = pj[v] - pc[v];
+#if FVS_STRICT
         gx[v] = gx[v] + c.x * diff * w;
         gy[v] = gy[v] + c.y * diff * w;
+#else
+        // coefficients premultiplied by the weight on the host
+        gx[v] = gx[v] + c.x * diff;
+        gy[v] = gy[v] + c.y * diff;
+#endif
         if (LIM) {
           pmin[v] = pj[v] < pmin[v] ? pj[v] : pmin[v];
           pmax[v] = pj[v] > pmax[v] ? pj[v] : pmax[v];
@@ -270,6 +333,9 @@ __device__ __forceinline__ void ghost_state(const DevView& d, int type, double t
 // ---------------------------------------------------------------------------
 // edge fluxes : one thread per edge slot
 // ---------------------------------------------------------------------------
+// SPEC: non-strict builds only, kappa = 0 and no limiter (phi = 1), where the
+// reconstruction reduces to p + (dx, dy).grad exactly
+template <bool SPEC>
 __global__ void __launch_bounds__(256) k_flux(const DevView d, double dts) {
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= d.nedge) return;
@@ -285,23 +351,31 @@ __global__ void __launch_bounds__(256) k_flux(const DevView d, double dts) {
   ld4(P, lr.x, pl);
   ld4(GX, lr.x, gxl);
   ld4(GY, lr.x, gyl);
-  const T phiL = PH[lr.x];
+  const T phiL = SPEC ? T(1) : PH[lr.x];
   if (e < d.nint) {
     // src/residual.f90:83-92
     T pr[4], gxr[4], gyr[4];
     ld4(P, lr.y, pr);
     ld4(GX, lr.y, gxr);
     ld4(GY, lr.y, gyr);
-    const T phiR = PH[lr.y];
     const T2 dr = ld2(d.edR, e);
-    const T kh = T(d.khalf), nkh = T(d.nkhalf), omk = T(d.omk);
+    if (SPEC) {
 #pragma unroll
-    for (int v = 0; v < 4; v++) {
-      const T gradC = pr[v] - pl[v];
-      const T gradL = dl.x * gxl[v] + dl.y * gyl[v];
-      const T gradR = dr.x * gxr[v] + dr.y * gyr[v];
-      pfL[v] = pl[v] + phiL * (kh * gradC + omk * gradL);
-      pfR[v] = pr[v] + phiR * (nkh * gradC + omk * gradR);
+      for (int v = 0; v < 4; v++) {
+        pfL[v] = pl[v] + (dl.x * gxl[v] + dl.y * gyl[v]);
+        pfR[v] = pr[v] + (dr.x * gxr[v] + dr.y * gyr[v]);
+      }
+    } else {
+      const T phiR = PH[lr.y];
+      const T kh = T(d.khalf), nkh = T(d.nkhalf), omk = T(d.omk);
+#pragma unroll
+      for (int v = 0; v < 4; v++) {
+        const T gradC = pr[v] - pl[v];
+        const T gradL = dl.x * gxl[v] + dl.y * gyl[v];
+        const T gradR = dr.x * gxr[v] + dr.y * gyr[v];
+        pfL[v] = pl[v] + phiL * (kh * gradC + omk * gradL);
+        pfR[v] = pr[v] + phiR * (nkh * gradC + omk * gradR);
+      }
     }
   } else {
     // src/residual.f90:128-137
@@ -312,7 +386,11 @@ __global__ void __launch_bounds__(256) k_flux(const DevView d, double dts) {
     ghost_state(d, d.ebtype[bi], d.tctl[1] + dts, xy.x, xy.y, n.x, n.y, pfL, pfR);
   }
   T flux[4], wsm;
+#if FVS_STRICT
   roe_flux(T(d.gamma), pfL, pfR, n.x, n.y, flux, wsm);
+#else
+  roe_flux_fast(T(d.gamma), T(d.gamma - 1.0), T(1.0 / (d.gamma - 1.0)), pfL, pfR, n.x, n.y, flux, wsm);
+#endif
 #pragma unroll
   for (int v = 0; v < 4; v++) flux[v] = flux[v] * af;
   st4(static_cast<T*>(d.eflux), e, flux);
@@ -322,6 +400,7 @@ __global__ void __launch_bounds__(256) k_flux(const DevView d, double dts) {
 // ---------------------------------------------------------------------------
 // per-cell gather of the edge slots in the reference's summation order
 // ---------------------------------------------------------------------------
+template <bool WS>
 __device__ __forceinline__ void gather_slot(const DevView& d, int s, double* r, double& ws) {
   if (s == 0) return;
   const int idx = (s > 0 ? s : -s) - 1;
@@ -334,25 +413,26 @@ __device__ __forceinline__ void gather_slot(const DevView& d, int s, double* r, 
 #pragma unroll
     for (int v = 0; v < 4; v++) r[v] = r[v] - double(f[v]);
   }
-  ws = ws + double(static_cast<const T*>(d.ews)[idx]);
+  if (WS) ws = ws + double(static_cast<const T*>(d.ews)[idx]);
 }
 
+template <bool WS>
 __device__ __forceinline__ void cell_residual(const DevView& d, int ic, double* res, double& ws) {
   double r[4] = {0.0, 0.0, 0.0, 0.0};
   ws = 0.0;
   const int4 cf = d.cflist[ic];
-  gather_slot(d, cf.x, r, ws);
-  gather_slot(d, cf.y, r, ws);
-  gather_slot(d, cf.z, r, ws);
-  gather_slot(d, cf.w, r, ws);
-#if FVS_MIXED
-  const double rv = d.rvol[ic];
-#pragma unroll
-  for (int v = 0; v < 4; v++) res[v] = -r[v] * rv;
-#else
+  gather_slot<WS>(d, cf.x, r, ws);
+  gather_slot<WS>(d, cf.y, r, ws);
+  gather_slot<WS>(d, cf.z, r, ws);
+  gather_slot<WS>(d, cf.w, r, ws);
+#if FVS_STRICT
   const double vol = d.vol[ic];
 #pragma unroll
   for (int v = 0; v < 4; v++) res[v] = -r[v] / vol;  // src/residual.f90:164-166
+#else
+  const double rv = -d.rvol[ic];
+#pragma unroll
+  for (int v = 0; v < 4; v++) res[v] = r[v] * rv;
 #endif
 }
 
@@ -363,6 +443,12 @@ __device__ __forceinline__ void cons2prim(double g, const double* u, T* p) {
   p[1] = float(u[1]) / r;
   p[2] = float(u[2]) / r;
   p[3] = float(g - 1.0) * (float(u[3]) - 0.5f * r * (p[1] * p[1] + p[2] * p[2]));
+#elif !FVS_STRICT
+  const double ri = 1.0 / u[0];
+  p[0] = u[0];
+  p[1] = u[1] * ri;
+  p[2] = u[2] * ri;
+  p[3] = (g - 1.0) * (u[3] - 0.5 * p[0] * (p[1] * p[1] + p[2] * p[2]));
 #else
   // cvar2pvar, src/data_solution.f90:78-84
   p[0] = u[0];
@@ -400,7 +486,8 @@ __global__ void __launch_bounds__(256) k_update(const DevView d, const StagePara
   double d2[4] = {0.0, 0.0, 0.0, 0.0};
   if (ic < d.nc) {
     double res[4], ws;
-    cell_residual(d, ic, res, ws);
+    if (sp.steady && sp.stage == 1) cell_residual<true>(d, ic, res, ws);
+    else cell_residual<false>(d, ic, res, ws);
     double h = sp.h;
     if (sp.steady) {
       double dtl;
@@ -479,7 +566,7 @@ __global__ void __launch_bounds__(256) k_residual_out(const DevView d) {
   const int ic = blockIdx.x * blockDim.x + threadIdx.x;
   if (ic >= d.nc) return;
   double res[4], ws;
-  cell_residual(d, ic, res, ws);
+  cell_residual<true>(d, ic, res, ws);
   st4(d.resid, ic, res);
   d.ws[ic] = ws;
 }
@@ -540,7 +627,11 @@ static void launch_gradient(const DevView& d, cudaStream_t s) {
   }
 }
 
-static void launch_flux(const DevView& d, double dts, cudaStream_t s) { k_flux<<<grid_of(d.nedge), 256, 0, s>>>(d, dts); }
+static void launch_flux(const DevView& d, double dts, cudaStream_t s) {
+  const bool spec = !FVS_STRICT && d.khalf == 0.0 && d.omk == 1.0 && d.limiter == FVS_LIM_NONE && !d.first_order;
+  if (spec) k_flux<true><<<grid_of(d.nedge), 256, 0, s>>>(d, dts);
+  else k_flux<false><<<grid_of(d.nedge), 256, 0, s>>>(d, dts);
+}
 
 static void launch_update(const DevView& d, const StageParams& sp, cudaStream_t s) {
   const unsigned g = grid_of(d.nc);
