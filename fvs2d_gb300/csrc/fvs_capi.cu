@@ -253,12 +253,13 @@ int build_device(fvs_handle* H) {
     if (!push(bcell_of[k], nint + k + 1)) return H->fail(FVS_ERR_MESH, "a cell has more than 4 flux contributions");
   // cell arrays in device order
   std::vector<double> vol(nc), rvol(nc);
-  std::vector<T> eps2(nc), cpos(8 * (size_t)nc, T(0));
+  std::vector<T> eps2(nc), cpos(8 * (size_t)nc, T(0)), rvolT(nc);
   std::vector<int8_t> nvrt(nc);
   for (int o = 0; o < nc; o++) {
     int dc = perm[o];
     vol[dc] = h.vol[o];
     rvol[dc] = 1.0 / h.vol[o];
+    rvolT[dc] = T(1.0 / h.vol[o]);
     eps2[dc] = T(h.eps2[o]);
     nvrt[dc] = h.nvrt[o];
     for (int k = 0; k < h.nvrt[o]; k++) {
@@ -308,17 +309,17 @@ int build_device(fvs_handle* H) {
   int8_t *dnv, *dsn;
   int *dsp, *dsc, *deb, *dperm;
   int2* dec;
-  T *t_eps2, *t_cpos, *t_coef, *t_w, *t_c0, *t_ce, *t_nrm, *t_area, *t_edL, *t_edR, *t_exy;
+  T *t_rvol, *t_eps2, *t_cpos, *t_coef, *t_w, *t_c0, *t_ce, *t_nrm, *t_area, *t_edL, *t_edR, *t_exy;
   ok = ok && H->upload(dvol, vol) && H->upload(drvol, rvol) && H->upload(dcf, cf) && H->upload(dnv, nvrt);
   ok = ok && H->upload(dsp, st_ptr) && H->upload(dsc, st_cell) && H->upload(dsn, st_node) && H->upload(dec, ecell);
   ok = ok && H->upload(deb, ebtype) && H->upload(dperm, perm);
-  ok = ok && H->upload(t_eps2, eps2) && H->upload(t_cpos, cpos) && H->upload(t_coef, st_coef) && H->upload(t_w, st_w);
+  ok = ok && H->upload(t_rvol, rvolT) && H->upload(t_eps2, eps2) && H->upload(t_cpos, cpos) && H->upload(t_coef, st_coef) && H->upload(t_w, st_w);
   ok = ok && H->upload(t_c0, coef0) && H->upload(t_ce, coefedg) && H->upload(t_nrm, enrm) && H->upload(t_area, earea);
   ok = ok && H->upload(t_edL, edL) && H->upload(t_edR, edR) && H->upload(t_exy, exy);
   H->d_perm = dperm;
   if (!ok) return H->fail(FVS_ERR_NOMEM, "device allocation or upload of the mesh failed");
   d.vol = dvol; d.rvol = drvol; d.cflist = dcf; d.nvrt = dnv; d.st_ptr = dsp; d.st_cell = dsc; d.st_node = dsn;
-  d.ecell = dec; d.ebtype = deb; d.eps2 = t_eps2; d.cpos = t_cpos; d.st_coef = t_coef; d.st_w = t_w; d.coef0 = t_c0;
+  d.ecell = dec; d.ebtype = deb; d.volT = t_rvol; d.eps2 = t_eps2; d.cpos = t_cpos; d.st_coef = t_coef; d.st_w = t_w; d.coef0 = t_c0;
   d.coefedg = t_ce; d.enrm = t_nrm; d.earea = t_area; d.edL = t_edL; d.edR = t_edR; d.exy = t_exy;
   // state and work arrays
   void* p;
@@ -551,6 +552,10 @@ int fvs_create(const fvs_mesh* mesh, const fvs_options* opt, fvs_handle** out) {
   d.nkhalf = -H->o.umuscl / 2.0;
   d.omk = 1.0 - H->o.umuscl;
   d.cfl = H->o.cfl;
+  d.gm1 = H->o.gamma - 1.0;
+  d.igm1 = 1.0 / (H->o.gamma - 1.0);
+  d.fgamma = float(d.gamma); d.fgm1 = float(d.gm1); d.figm1 = float(d.igm1);
+  d.fkhalf = float(d.khalf); d.fnkhalf = float(d.nkhalf); d.fomk = float(d.omk);
   d.limiter = H->o.limiter;
   d.grad_method = H->o.grad_method;
   d.first_order = H->o.reconst == FVS_RECON_UPWIND1;

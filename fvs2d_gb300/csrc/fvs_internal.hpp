@@ -120,6 +120,10 @@ struct DevView {
   double* tctl = nullptr;         // [0] = t1, [1] = told of the current step
   // scheme
   double gamma = 1.4, khalf = 0, nkhalf = 0, omk = 1, cfl = 1, dt = 0;
+  double gm1 = 0.4, igm1 = 2.5;  // gamma-1 and 1/(gamma-1)
+  // the same constants rounded once on the host for the FP32 kernels
+  float fgamma = 1.4f, fgm1 = 0.4f, figm1 = 2.5f, fkhalf = 0, fnkhalf = 0, fomk = 1;
+  const void* volT = nullptr;    // [nc] 1/vol in the compute type (GG gradients)
   int limiter = 0, grad_method = 3, first_order = 0, vortex = 0;
   double vx = 0, vy = 0, vkappa = 0, vinf[4] = {0, 0, 0, 0};
   double pinf[4] = {0, 0, 0, 0};

@@ -53,6 +53,45 @@ __device__ __forceinline__ T2 ld2(const void* p, int i) {
   return reinterpret_cast<const T2*>(p)[i];
 }
 
+// scheme constants in the compute type, rounded once on the host
+#if FVS_MIXED
+#define TP(name) (d.f##name)
+#else
+#define TP(name) (d.name)
+#endif
+
+// Exact FP32 -> FP64 conversion on the integer pipe (the FP64 pipe, 2 ops per
+// clock per SM on GB300, is the scarce resource of the update kernel).
+// FP32 subnormals (|x| < 1.2e-38) become signed zero; Inf/NaN are kept.
+__device__ __forceinline__ double f2d_bits(float f) {
+  const unsigned int b = __float_as_uint(f);
+  const unsigned int e = (b >> 23) & 0xffu;
+  const unsigned int sign = b & 0x80000000u;
+  const unsigned int de = e == 0u ? 0u : (e == 0xffu ? 0x7ffu : e + 896u);
+  const unsigned int m = e == 0u ? 0u : (b & 0x7fffffu);
+  const unsigned int hi = sign | (de << 20) | (m >> 3);
+  const unsigned int lo = m << 29;
+  return __hiloint2double((int)hi, (int)lo);
+}
+
+// FP64 -> FP32 rounded to nearest even, on the integer pipe.  Results below
+// the FP32 normal range flush to signed zero, above it become Inf.
+__device__ __forceinline__ float d2f_bits(double x) {
+  const unsigned int hi = (unsigned int)__double2hiint(x), lo = (unsigned int)__double2loint(x);
+  const unsigned int sign = hi & 0x80000000u;
+  const int e = (int)((hi >> 20) & 0x7ffu);
+  if (e == 0x7ff) return __uint_as_float(sign | 0x7f800000u | ((hi & 0xfffffu) ? 0x400000u : 0u));
+  const int fe = e - 896;
+  if (fe <= 0) return __uint_as_float(sign);
+  // 23 kept mantissa bits: 20 from hi, 3 from the top of lo; 29 dropped bits
+  unsigned int mant = ((hi & 0xfffffu) << 3) | (lo >> 29);
+  const unsigned int rem = lo & 0x1fffffffu;
+  unsigned int r = ((unsigned int)fe << 23) + mant;
+  if (rem > 0x10000000u || (rem == 0x10000000u && (mant & 1u))) r += 1u;  // carry may bump the exponent
+  if (r >= 0x7f800000u) return __uint_as_float(sign | 0x7f800000u);
+  return __uint_as_float(sign | r);
+}
+
 __device__ __forceinline__ double dsqrt_(double x) { return sqrt(x); }
 __device__ __forceinline__ float dsqrt_(float x) { return sqrtf(x); }
 __device__ __forceinline__ double dabs_(double x) { return fabs(x); }
@@ -232,9 +271,15 @@ __global__ void __launch_bounds__(256) k_gradient(const DevView d) {
 #pragma unroll
       for (int v = 0; v < 4; v++) { gx[v] = gx[v] + c.x * pj[v]; gy[v] = gy[v] + c.y * pj[v]; }
     }
-    const T vol = T(d.vol[ic]);
+#if FVS_STRICT
+    const T vol = d.vol[ic];
 #pragma unroll
     for (int v = 0; v < 4; v++) { gx[v] = gx[v] / vol; gy[v] = gy[v] / vol; }
+#else
+    const T rv = static_cast<const T*>(d.volT)[ic];
+#pragma unroll
+    for (int v = 0; v < 4; v++) { gx[v] = gx[v] * rv; gy[v] = gy[v] * rv; }
+#endif
   } else {
     // grad_ggnb, src/gradient_ggnb.f90:190-207
     const T2 c0 = ld2(d.coef0, ic);
@@ -249,9 +294,15 @@ __global__ void __launch_bounds__(256) k_gradient(const DevView d) {
 #pragma unroll
       for (int v = 0; v < 4; v++) { gx[v] = gx[v] + ce.x * cn * pj[v]; gy[v] = gy[v] + ce.y * cn * pj[v]; }
     }
-    const T vol = T(d.vol[ic]);
+#if FVS_STRICT
+    const T vol = d.vol[ic];
 #pragma unroll
     for (int v = 0; v < 4; v++) { gx[v] = gx[v] / vol; gy[v] = gy[v] / vol; }
+#else
+    const T rv = static_cast<const T*>(d.volT)[ic];
+#pragma unroll
+    for (int v = 0; v < 4; v++) { gx[v] = gx[v] * rv; gy[v] = gy[v] * rv; }
+#endif
   }
   st4(static_cast<T*>(d.Gx), ic, gx);
   st4(static_cast<T*>(d.Gy), ic, gy);
@@ -367,7 +418,7 @@ __global__ void __launch_bounds__(256) k_flux(const DevView d, double dts) {
       }
     } else {
       const T phiR = PH[lr.y];
-      const T kh = T(d.khalf), nkh = T(d.nkhalf), omk = T(d.omk);
+      const T kh = TP(khalf), nkh = TP(nkhalf), omk = TP(omk);
 #pragma unroll
       for (int v = 0; v < 4; v++) {
         const T gradC = pr[v] - pl[v];
@@ -389,7 +440,7 @@ __global__ void __launch_bounds__(256) k_flux(const DevView d, double dts) {
 #if FVS_STRICT
   roe_flux(T(d.gamma), pfL, pfR, n.x, n.y, flux, wsm);
 #else
-  roe_flux_fast(T(d.gamma), T(d.gamma - 1.0), T(1.0 / (d.gamma - 1.0)), pfL, pfR, n.x, n.y, flux, wsm);
+  roe_flux_fast(TP(gamma), TP(gm1), TP(igm1), pfL, pfR, n.x, n.y, flux, wsm);
 #endif
 #pragma unroll
   for (int v = 0; v < 4; v++) flux[v] = flux[v] * af;
@@ -400,20 +451,53 @@ __global__ void __launch_bounds__(256) k_flux(const DevView d, double dts) {
 // ---------------------------------------------------------------------------
 // per-cell gather of the edge slots in the reference's summation order
 // ---------------------------------------------------------------------------
+#if FVS_MIXED
+// FP32 flux slots summed with an error-free transformation (TwoSum): hi + lo
+// equals the exact sum of the slots to ~2^-48 relative, then one FP64 add per
+// component; the result matches an FP64 accumulation of the FP32 fluxes.
+__device__ __forceinline__ void two_sum(float& hi, float& lo, float x) {
+  const float s = hi + x;
+  const float bp = s - hi;
+  lo += (hi - (s - bp)) + (x - bp);
+  hi = s;
+}
+
+template <bool WS>
+__device__ __forceinline__ void cell_residual(const DevView& d, int ic, double* res, double& ws) {
+  float hi[4] = {0.f, 0.f, 0.f, 0.f}, lo[4] = {0.f, 0.f, 0.f, 0.f}, wh = 0.f, wl = 0.f;
+  const int4 cf = d.cflist[ic];
+  const int sl[4] = {cf.x, cf.y, cf.z, cf.w};
+#pragma unroll
+  for (int j = 0; j < 4; j++) {
+    const int s = sl[j];
+    if (s == 0) continue;
+    const int idx = (s > 0 ? s : -s) - 1;
+    float f[4];
+    ld4(static_cast<const float*>(d.eflux), idx, f);
+#pragma unroll
+    for (int v = 0; v < 4; v++) two_sum(hi[v], lo[v], s > 0 ? f[v] : -f[v]);
+    if (WS) two_sum(wh, wl, static_cast<const float*>(d.ews)[idx]);
+  }
+  const double rv = -d.rvol[ic];
+#pragma unroll
+  for (int v = 0; v < 4; v++) res[v] = (f2d_bits(hi[v]) + f2d_bits(lo[v])) * rv;
+  ws = WS ? f2d_bits(wh) + f2d_bits(wl) : 0.0;
+}
+#else
 template <bool WS>
 __device__ __forceinline__ void gather_slot(const DevView& d, int s, double* r, double& ws) {
   if (s == 0) return;
   const int idx = (s > 0 ? s : -s) - 1;
-  T f[4];
-  ld4(static_cast<const T*>(d.eflux), idx, f);
+  double f[4];
+  ld4(static_cast<const double*>(d.eflux), idx, f);
   if (s > 0) {
 #pragma unroll
-    for (int v = 0; v < 4; v++) r[v] = r[v] + double(f[v]);
+    for (int v = 0; v < 4; v++) r[v] = r[v] + f[v];
   } else {
 #pragma unroll
-    for (int v = 0; v < 4; v++) r[v] = r[v] - double(f[v]);
+    for (int v = 0; v < 4; v++) r[v] = r[v] - f[v];
   }
-  if (WS) ws = ws + double(static_cast<const T*>(d.ews)[idx]);
+  if (WS) ws = ws + static_cast<const double*>(d.ews)[idx];
 }
 
 template <bool WS>
@@ -435,49 +519,49 @@ __device__ __forceinline__ void cell_residual(const DevView& d, int ic, double* 
   for (int v = 0; v < 4; v++) res[v] = r[v] * rv;
 #endif
 }
+#endif
 
-__device__ __forceinline__ void cons2prim(double g, const double* u, T* p) {
+// g = gamma - 1 in the compute type
+__device__ __forceinline__ void cons2prim(T g, const double* u, T* p) {
 #if FVS_MIXED
-  const float r = float(u[0]);
+  const float r = d2f_bits(u[0]), ri = 1.0f / r;
   p[0] = r;
-  p[1] = float(u[1]) / r;
-  p[2] = float(u[2]) / r;
-  p[3] = float(g - 1.0) * (float(u[3]) - 0.5f * r * (p[1] * p[1] + p[2] * p[2]));
+  p[1] = d2f_bits(u[1]) * ri;
+  p[2] = d2f_bits(u[2]) * ri;
+  p[3] = g * (d2f_bits(u[3]) - 0.5f * r * (p[1] * p[1] + p[2] * p[2]));
 #elif !FVS_STRICT
   const double ri = 1.0 / u[0];
   p[0] = u[0];
   p[1] = u[1] * ri;
   p[2] = u[2] * ri;
-  p[3] = (g - 1.0) * (u[3] - 0.5 * p[0] * (p[1] * p[1] + p[2] * p[2]));
+  p[3] = g * (u[3] - 0.5 * p[0] * (p[1] * p[1] + p[2] * p[2]));
 #else
   // cvar2pvar, src/data_solution.f90:78-84
   p[0] = u[0];
   p[1] = u[1] / u[0];
   p[2] = u[2] / u[0];
-  p[3] = (g - 1.0) * (u[3] - 0.5 * p[0] * (p[1] * p[1] + p[2] * p[2]));
+  p[3] = g * (u[3] - 0.5 * p[0] * (p[1] * p[1] + p[2] * p[2]));
 #endif
 }
 
-// deterministic block sum of 4 doubles; thread 0 of each block writes out
-__device__ __forceinline__ void block_sum4(double* v, double* out) {
-  __shared__ double sh[8][4];
+// deterministic block sum of 4 doubles (shared-memory tree: one add per
+// element instead of five shuffle-adds per lane); thread 0 gets the sums
+__device__ __forceinline__ void block_sum4(const double* v, double* out) {
+  __shared__ double sh[4][256];
+  const int t = threadIdx.x;
 #pragma unroll
-  for (int k = 0; k < 4; k++)
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_down_sync(0xffffffffu, v[k], o);
-  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-  if (l == 0)
-#pragma unroll
-    for (int k = 0; k < 4; k++) sh[w][k] = v[k];
+  for (int k = 0; k < 4; k++) sh[k][t] = v[k];
   __syncthreads();
-  if (threadIdx.x == 0) {
-    const int nw = blockDim.x >> 5;
-    for (int k = 0; k < 4; k++) {
-      double s = 0.0;
-      for (int i = 0; i < nw; i++) s += sh[i][k];
-      out[k] = s;
+  for (int w = blockDim.x >> 1; w > 0; w >>= 1) {
+    if (t < w) {
+#pragma unroll
+      for (int k = 0; k < 4; k++) sh[k][t] += sh[k][t + w];
     }
+    __syncthreads();
   }
+  if (t == 0)
+#pragma unroll
+    for (int k = 0; k < 4; k++) out[k] = sh[k][0];
 }
 
 template <int MODE>
@@ -542,7 +626,7 @@ __global__ void __launch_bounds__(256) k_update(const DevView d, const StagePara
     }
     st4(d.U, ic, u);
     T p[4];
-    cons2prim(d.gamma, u, p);
+    cons2prim(TP(gm1), u, p);
     st4(static_cast<T*>(d.Pv), ic, p);
     if (sp.last) {
 #pragma unroll
@@ -577,7 +661,7 @@ __global__ void __launch_bounds__(256) k_cvar2pvar(const DevView d) {
   double u[4];
   T p[4];
   ld4(d.U, ic, u);
-  cons2prim(d.gamma, u, p);
+  cons2prim(TP(gm1), u, p);
   st4(static_cast<T*>(d.Pv), ic, p);
 }
 
