@@ -28,6 +28,7 @@ UNITS = {
     "fvs_kern_strict.cu": ["-fmad=false"],
     "fvs_kern_fast.cu": ["-fmad=true"],
     "fvs_kern_mixed.cu": ["-fmad=true"],
+    "fvs_noalloc.cu": [],
 }
 HEADERS = ["fvs_internal.hpp", "fvs_kernels.cuh"]
 

@@ -85,6 +85,7 @@ SIGNATURES = {
     "fvs_profile_step": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_int32), C.c_char_p, C.POINTER(C.c_float)]),
     "fvs_launches_per_step": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32)]),
     "fvs_device_state": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
+    "fvs_rms_delta_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p]),
 }
 
 _LIB = None

@@ -208,6 +208,24 @@ int fvs_launches_per_step(const fvs_handle* h, int32_t* n);
  * old->new (host copy, 0-based) for callers that keep data on the device. */
 int fvs_device_state(fvs_handle* h, void** dptr);
 
+/* ---- allocation-free residual norm ---------------------------------------
+ * No counterpart in the reference: an addition for callers that cannot
+ * allocate device memory where they need the norm (hosts whose device memory
+ * is reserved up front by another allocator, loops that must not pay
+ * cudaMalloc's implicit synchronisation).  Computes what fvs_time_integration
+ * logs per step, RMS over cells of |U - U0| per component, from two device
+ * arrays [ncells][4] into dev_norm4[4], on `stream` (a cudaStream_t; NULL =
+ * the legacy default stream).  Allocates nothing: its block partial sums live
+ * in a fixed device array of FVS_NOALLOC_MAX_BLOCKS x 4 doubles (256 KB per
+ * GPU that loads the library, held until exit), so ncells is limited to
+ * FVS_NOALLOC_MAX_CELLS; larger inputs return FVS_ERR_INVALID.  Every call on
+ * a device shares that array: calls that overlap on the GPU race.  The first
+ * call on a device (with that device current) looks up the array's address;
+ * make it before any stream capture.  The call is asynchronous on `stream`. */
+#define FVS_NOALLOC_MAX_BLOCKS 8192
+#define FVS_NOALLOC_MAX_CELLS (FVS_NOALLOC_MAX_BLOCKS * 256)
+int fvs_rms_delta_noalloc(const double* dev_u, const double* dev_u0, int32_t ncells, double* dev_norm4, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
