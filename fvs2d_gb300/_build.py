@@ -29,8 +29,9 @@ UNITS = {
     "fvs_kern_fast.cu": ["-fmad=true"],
     "fvs_kern_mixed.cu": ["-fmad=true"],
     "fvs_noalloc.cu": [],
+    "fvs_batch.cu": [],
 }
-HEADERS = ["fvs_internal.hpp", "fvs_kernels.cuh"]
+HEADERS = ["fvs_internal.hpp", "fvs_kernels.cuh", "fvs_layout.hpp"]
 
 
 def nvcc() -> str:

@@ -1,0 +1,99 @@
+"""Batched independent cases through the C-ABI (fvs_batch_*).
+
+All cases share the scheme; each has its own mesh, Mach number and angle of
+attack.  One cooperative persistent kernel advances every active case per
+chunk of steps; converged cases leave the work lists.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import capi
+from .solver import FvsError
+
+
+class Batch:
+    def __init__(self, meshes, options, host_threads: int = 0):
+        if len(meshes) != len(options) or not meshes:
+            raise ValueError("one Options per mesh")
+        self._lib = capi.load()
+        self._arrays = [capi.MeshArrays(m) for m in meshes]
+        self._meshes = (capi.FvsMesh * len(meshes))(*[a.struct for a in self._arrays])
+        self._opts = (capi.FvsOptions * len(options))(*[o.to_struct() for o in options])
+        h = C.c_void_p()
+        rc = self._lib.fvs_batch_create(self._meshes, self._opts, len(meshes), int(host_threads), C.byref(h))
+        if rc != capi.FVS_OK:
+            raise FvsError(rc, self._lib.fvs_batch_last_error(None).decode())
+        self._h = h
+        self.ncases = len(meshes)
+        self.case_cells = [m.ncells for m in meshes]
+
+    def _check(self, rc):
+        if rc != capi.FVS_OK:
+            raise FvsError(rc, self._lib.fvs_batch_last_error(self._h).decode())
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.fvs_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def info(self) -> dict:
+        nc, ne = C.c_int32(0), C.c_int32(0)
+        launch = (C.c_int32 * 4)()
+        self._check(self._lib.fvs_batch_info(self._h, C.byref(nc), C.byref(ne), launch))
+        return {"ncells": nc.value, "nedges": ne.value, "block": launch[0], "tile": launch[1],
+                "blocks_per_sm": launch[2], "graph": bool(launch[3])}
+
+    def initialize_solution(self):
+        self._check(self._lib.fvs_batch_init_state(self._h))
+
+    def set_state(self, icase: int, cvar) -> None:
+        a = np.ascontiguousarray(cvar, np.float64).reshape(self.case_cells[icase], 4)
+        self._check(self._lib.fvs_batch_set_state(self._h, int(icase), capi.ptr(a)))
+
+    def get_state(self, icase: int) -> np.ndarray:
+        out = np.empty((self.case_cells[icase], 4), np.float64)
+        self._check(self._lib.fvs_batch_get_state(self._h, int(icase), capi.ptr(out)))
+        return out
+
+    def steps(self, nsteps: int):
+        """nsteps steps of all cases; returns (norms [ncases][nsteps][4], ms)."""
+        norms = np.empty((self.ncases, nsteps, 4), np.float64)
+        ms = C.c_float(0)
+        self._check(self._lib.fvs_batch_steps(self._h, int(nsteps), capi.ptr(norms), C.byref(ms)))
+        return norms, ms.value
+
+    def autotune(self, trial_steps: int = 3) -> float:
+        ms = C.c_float(0)
+        self._check(self._lib.fvs_batch_autotune(self._h, int(trial_steps), C.byref(ms)))
+        return ms.value
+
+    def set_launch(self, block: int, tile: int, blocks_per_sm: int):
+        self._check(self._lib.fvs_batch_set_launch(self._h, block, tile, blocks_per_sm))
+
+    def set_barrier_budget(self, seconds: float):
+        self._check(self._lib.fvs_batch_set_barrier_budget(self._h, float(seconds)))
+
+    def run_to_drop(self, max_steps: int, drop: float = 1e-10, chunk: int = 50):
+        """Returns (steps_done [ncases], first [ncases,4], last [ncases,4], ms)."""
+        done = np.zeros(self.ncases, np.int32)
+        first = np.zeros((self.ncases, 4))
+        last = np.zeros((self.ncases, 4))
+        ms = C.c_float(0)
+        self._check(self._lib.fvs_batch_run_to_drop(self._h, int(max_steps), float(drop), int(chunk), capi.ptr(done),
+                                                    capi.ptr(first), capi.ptr(last), C.byref(ms)))
+        return done, first, last, ms.value

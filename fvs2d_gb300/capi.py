@@ -85,6 +85,19 @@ SIGNATURES = {
     "fvs_profile_step": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_int32), C.c_char_p, C.POINTER(C.c_float)]),
     "fvs_launches_per_step": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32)]),
     "fvs_device_state": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
+    "fvs_batch_create": (C.c_int, [C.POINTER(FvsMesh), C.POINTER(FvsOptions), C.c_int32, C.c_int32, C.POINTER(C.c_void_p)]),
+    "fvs_batch_destroy": (None, [C.c_void_p]),
+    "fvs_batch_last_error": (C.c_char_p, [C.c_void_p]),
+    "fvs_batch_info": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.c_void_p]),
+    "fvs_batch_init_state": (C.c_int, [C.c_void_p]),
+    "fvs_batch_set_state": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p]),
+    "fvs_batch_get_state": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p]),
+    "fvs_batch_autotune": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_float)]),
+    "fvs_batch_set_launch": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32]),
+    "fvs_batch_set_barrier_budget": (C.c_int, [C.c_void_p, C.c_double]),
+    "fvs_batch_steps": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.POINTER(C.c_float)]),
+    "fvs_batch_run_to_drop": (C.c_int, [C.c_void_p, C.c_int32, C.c_double, C.c_int32, C.c_void_p, C.c_void_p,
+                                        C.c_void_p, C.POINTER(C.c_float)]),
     "fvs_rms_delta_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p]),
 }
 

@@ -1,0 +1,593 @@
+// fvs_batch.cu — many independent cases in one persistent launch.
+//
+// The cases' meshes are packed as a disjoint union (each case's cells and
+// edge slots contiguous, fvs_layout.hpp), so the per-item device code of the
+// single-mesh path serves unchanged; what is per case is the free stream
+// (boundary records carry the case index), the residual norm (cell tiles
+// never straddle cases) and convergence (converged cases are dropped from
+// the tile lists).  One cooperative launch of k_persistent advances all
+// active cases by a chunk of RK steps with bounded grid barriers between the
+// phases; the launch is captured once in a CUDA graph and replayed.  The
+// launch shape (block size, tile length, resident blocks per SM) comes from
+// a small autotuner that times the candidates on the batch itself.
+//
+// The reference runs one case per process (src/fvs2d.f90); the batch has no
+// counterpart there beyond running time_integration on each case.
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "fvs_internal.hpp"
+#include "fvs_layout.hpp"
+
+using namespace fvs;
+
+namespace {
+
+thread_local std::string g_batch_create_error;
+
+__global__ void kb_scatter_in(const double* __restrict__ ref, const int* __restrict__ perm, double* __restrict__ dev, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double2* s = reinterpret_cast<const double2*>(ref) + 2 * (size_t)i;
+  double2* t = reinterpret_cast<double2*>(dev) + 2 * (size_t)perm[i];
+  t[0] = s[0];
+  t[1] = s[1];
+}
+
+__global__ void kb_gather_out(const double* __restrict__ dev, const int* __restrict__ perm, double* __restrict__ ref, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double2* s = reinterpret_cast<const double2*>(dev) + 2 * (size_t)perm[i];
+  double2* t = reinterpret_cast<double2*>(ref) + 2 * (size_t)i;
+  t[0] = s[0];
+  t[1] = s[1];
+}
+
+bool same_scheme(const fvs_options& a, const fvs_options& b) {
+  return a.gamma == b.gamma && a.dt == b.dt && a.cfl == b.cfl && a.steady == b.steady && a.vortex == b.vortex &&
+         a.ntstart == b.ntstart && a.grad_method == b.grad_method && a.lsq_stencil == b.lsq_stencil &&
+         a.lsq_pow == b.lsq_pow && a.limiter == b.limiter && a.reconst == b.reconst && a.umuscl == b.umuscl &&
+         a.flux == b.flux && a.rk_nstages == b.rk_nstages && a.rk_order == b.rk_order && a.ssprk == b.ssprk &&
+         a.precision == b.precision;
+}
+
+}  // namespace
+
+struct fvs_batch {
+  int ncases = 0;
+  std::vector<HostMesh> hm;
+  std::vector<fvs_options> opt;
+  fvs_options base;
+  std::string err;
+  const KernelSet* ks = nullptr;
+  bool mixed = false;
+  cudaStream_t stream = nullptr;
+  DeviceArena arena;
+  DevView d;
+  int nc = 0, ne = 0;
+  std::vector<int> coff, eoff, cnum, enumv;  // per-case cell / edge-slot ranges
+  std::vector<double> pinf;                 // [ncases][4]
+  int* d_perm = nullptr;                    // concatenated reference -> device cell maps
+  std::vector<int> ref_off;                 // offset of each case in d_perm
+  double* d_stage = nullptr;
+  double* d_backup = nullptr;               // state saved around the autotuner
+  std::vector<StageParams> stages;
+  // launch shape and plan
+  int block = 256, tile = 1024, bps = 1, nsm = 0;
+  int4* d_cell_tiles = nullptr;
+  int2* d_edge_tiles = nullptr;
+  int4* d_case_tiles = nullptr;
+  double* d_tile_partials = nullptr;
+  double* d_case_norms = nullptr;
+  int* d_step0 = nullptr;
+  GridBarrier* d_bar = nullptr;
+  int cap_cell_tiles = 0, cap_edge_tiles = 0;
+  int norm_cap = 1024;
+  double budget_s = 4.0;
+  PersistPlan plan;
+  std::vector<char> active;
+  cudaGraphExec_t graph = nullptr;
+  int graph_steps = -1;
+  bool plan_dirty = true, use_graph = true;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  int* h_step0 = nullptr;
+
+  ~fvs_batch() {
+    if (graph) cudaGraphExecDestroy(graph);
+    if (ev0) cudaEventDestroy(ev0);
+    if (ev1) cudaEventDestroy(ev1);
+    if (h_step0) cudaFreeHost(h_step0);
+    arena.release();
+    if (stream) cudaStreamDestroy(stream);
+  }
+  int fail(int code, const std::string& m) {
+    err = m;
+    return code;
+  }
+  int cuda_fail(cudaError_t e, const char* where) {
+    err = std::string(where) + ": " + cudaGetErrorString(e);
+    return FVS_ERR_CUDA;
+  }
+};
+
+namespace {
+
+template <typename T>
+int build_batch_device(fvs_batch* B) {
+  Layout<T> L;
+  std::string err;
+  const bool fold_w = B->base.precision != FVS_PREC_FP64_STRICT;
+  for (int c = 0; c < B->ncases; c++) {
+    int rc = append_case(L, B->hm[c], fold_w, c, err);
+    if (rc) return B->fail(rc, "case " + std::to_string(c) + ": " + err);
+    B->coff.push_back(L.case_coff[c]);
+    B->eoff.push_back(L.case_eoff[c]);
+    B->cnum.push_back(B->hm[c].nc);
+    B->enumv.push_back((int)(B->hm[c].edge_intr.size() + B->hm[c].b_edge.size()));
+  }
+  B->nc = L.nc;
+  B->ne = L.ne;
+  B->ref_off = B->coff;  // L.perm is appended case by case in the same order
+  DevView& d = B->d;
+  if (!upload_layout(B->arena, L, d) || !B->arena.upload(B->d_perm, L.perm))
+    return B->fail(FVS_ERR_NOMEM, "device allocation or upload of the batch meshes failed");
+  double* dp = nullptr;
+  if (!B->arena.upload(dp, B->pinf)) return B->fail(FVS_ERR_NOMEM, "upload of the free streams failed");
+  d.case_pinf = dp;
+  void* p;
+  const int nblk = (L.nc + 255) / 256;
+  bool ok = alloc_work<T>(B->arena, d, L.nc, L.ne, nblk, 16);
+  ok = ok && B->arena.alloc(p, 32 * (size_t)L.nc);
+  B->d_stage = static_cast<double*>(p);
+  ok = ok && B->arena.alloc(p, 32 * (size_t)L.nc);
+  B->d_backup = static_cast<double*>(p);
+  ok = ok && B->arena.alloc(p, 32 * (size_t)B->ncases * B->norm_cap);
+  B->d_case_norms = static_cast<double*>(p);
+  ok = ok && B->arena.alloc(p, sizeof(GridBarrier));
+  B->d_bar = static_cast<GridBarrier*>(p);
+  ok = ok && B->arena.alloc(p, 16);
+  B->d_step0 = static_cast<int*>(p);
+  ok = ok && B->arena.alloc(p, 16 * (size_t)B->ncases);
+  B->d_case_tiles = static_cast<int4*>(p);
+  if (!ok) return B->fail(FVS_ERR_NOMEM, "device allocation of the batch state failed");
+  std::vector<T> phi0(L.nc, T(B->base.reconst == FVS_RECON_UPWIND1 ? 0.0 : 1.0));
+  if (cudaMemcpy(d.phi, phi0.data(), sizeof(T) * L.nc, cudaMemcpyHostToDevice) != cudaSuccess)
+    return B->fail(FVS_ERR_CUDA, "phi upload failed");
+  std::vector<double> dtl(L.nc, B->base.dt);
+  if (cudaMemcpy(d.dtl, dtl.data(), 8 * dtl.size(), cudaMemcpyHostToDevice) != cudaSuccess)
+    return B->fail(FVS_ERR_CUDA, "dt upload failed");
+  return FVS_OK;
+}
+
+void set_batch_stages(fvs_batch* B) {
+  const fvs_options& o = B->base;
+  double hr[5], c[5], dts[5];
+  rk_coefficients(o, o.dt, hr, c, dts);
+  B->stages.clear();
+  const int ns = o.rk_nstages;
+  for (int k = 1; k <= ns; k++) {
+    StageParams sp;
+    sp.stage = k; sp.nstages = ns; sp.steady = o.steady; sp.last = (k == ns);
+    sp.mode = (ns == 3 && o.ssprk) ? MODE_SSP3 : (o.ssprk ? MODE_SSP42 : MODE_RK);
+    sp.h = hr[k]; sp.coef = c[k]; sp.dts = dts[k];
+    if (sp.mode == MODE_SSP42) sp.cst = (k == 4) ? 1.0 / 4.0 : 1.0 / 3.0;
+    else if (sp.mode == MODE_RK) sp.cst = (k == 3) ? 1.0 : (k == 4 ? 1.0 / 6.0 : 1.0 / 2.0);
+    else sp.cst = 1.0;
+    if (sp.mode == MODE_SSP3) {
+      static const double A[4] = {0, 0.0, 0.75, 1.0 / 3.0}, Bw[4] = {0, 1.0, 0.25, 2.0 / 3.0};
+      sp.a = A[k]; sp.b = Bw[k];
+    }
+    B->stages.push_back(sp);
+  }
+  B->d.dt = o.dt;
+}
+
+// tile lists of the active cases for the current tile length
+int build_plan(fvs_batch* B) {
+  std::vector<int4> ct, cases;
+  std::vector<int2> et;
+  for (int c = 0; c < B->ncases; c++) {
+    if (!B->active[c]) continue;
+    const int first = (int)ct.size();
+    for (int a = B->coff[c]; a < B->coff[c] + B->cnum[c]; a += B->tile)
+      ct.push_back(make_int4(a, std::min(a + B->tile, B->coff[c] + B->cnum[c]), c, 0));
+    for (int a = B->eoff[c]; a < B->eoff[c] + B->enumv[c]; a += B->tile)
+      et.push_back(make_int2(a, std::min(a + B->tile, B->eoff[c] + B->enumv[c])));
+    cases.push_back(make_int4(c, first, (int)ct.size(), B->cnum[c]));
+  }
+  void* p;
+  if ((int)ct.size() > B->cap_cell_tiles) {
+    const int cap = (int)ct.size() * 2;
+    if (!B->arena.alloc(p, 16 * (size_t)cap)) return B->fail(FVS_ERR_NOMEM, "tile list allocation");
+    B->d_cell_tiles = static_cast<int4*>(p);
+    if (!B->arena.alloc(p, 32 * (size_t)cap)) return B->fail(FVS_ERR_NOMEM, "tile partial allocation");
+    B->d_tile_partials = static_cast<double*>(p);
+    B->cap_cell_tiles = cap;
+  }
+  if ((int)et.size() > B->cap_edge_tiles) {
+    const int cap = (int)et.size() * 2;
+    if (!B->arena.alloc(p, 8 * (size_t)cap)) return B->fail(FVS_ERR_NOMEM, "tile list allocation");
+    B->d_edge_tiles = static_cast<int2*>(p);
+    B->cap_edge_tiles = cap;
+  }
+  cudaError_t e = cudaSuccess;
+  if (!ct.empty()) e = cudaMemcpy(B->d_cell_tiles, ct.data(), 16 * ct.size(), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && !et.empty()) e = cudaMemcpy(B->d_edge_tiles, et.data(), 8 * et.size(), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && !cases.empty()) e = cudaMemcpy(B->d_case_tiles, cases.data(), 16 * cases.size(), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return B->cuda_fail(e, "plan upload");
+  PersistPlan& P = B->plan;
+  P.nstages = (int)B->stages.size();
+  for (int k = 0; k < P.nstages; k++) P.sp[k] = B->stages[k];
+  P.t1 = 0.0;
+  P.step0_dev = B->d_step0;
+  P.cell_tiles = B->d_cell_tiles;
+  P.ncell_tiles = (int)ct.size();
+  P.edge_tiles = B->d_edge_tiles;
+  P.nedge_tiles = (int)et.size();
+  P.case_tiles = B->d_case_tiles;
+  P.ncase_active = (int)cases.size();
+  P.tile_partials = B->d_tile_partials;
+  P.case_norms = B->d_case_norms;
+  P.norm_cap = B->norm_cap;
+  P.bar = B->d_bar;
+  int clk = 0;
+  cudaDeviceGetAttribute(&clk, cudaDevAttrClockRate, 0);
+  P.budget = (long long)(B->budget_s * (clk > 0 ? clk : 2000000) * 1000.0);
+  if (B->graph) {
+    cudaGraphExecDestroy(B->graph);
+    B->graph = nullptr;
+  }
+  B->graph_steps = -1;
+  B->plan_dirty = false;
+  return FVS_OK;
+}
+
+int grid_size(fvs_batch* B) {
+  const int occ = B->ks->persistent_occupancy(B->d, B->block);
+  return std::max(1, std::min(B->bps, occ)) * B->nsm;
+}
+
+// one chunk of nsteps steps starting at global step step0 (graph replay)
+int launch_chunk(fvs_batch* B, int nsteps, int step0) {
+  if (B->plan_dirty) {
+    int rc = build_plan(B);
+    if (rc) return rc;
+  }
+  if (B->plan.ncell_tiles == 0) return FVS_OK;
+  *B->h_step0 = step0;
+  cudaError_t e = cudaMemcpyAsync(B->d_step0, B->h_step0, sizeof(int), cudaMemcpyHostToDevice, B->stream);
+  if (e != cudaSuccess) return B->cuda_fail(e, "step upload");
+  const int grid = grid_size(B);
+  B->plan.nsteps = nsteps;
+  if (B->use_graph && B->graph_steps != nsteps) {
+    if (B->graph) { cudaGraphExecDestroy(B->graph); B->graph = nullptr; }
+    cudaGraph_t g;
+    e = cudaStreamBeginCapture(B->stream, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+      cudaMemsetAsync(B->d_bar, 0, sizeof(GridBarrier), B->stream);
+      cudaError_t le = B->ks->persistent(B->d, B->plan, grid, B->block, B->stream);
+      e = cudaStreamEndCapture(B->stream, &g);
+      if (le == cudaSuccess && e == cudaSuccess) {
+        e = cudaGraphInstantiate(&B->graph, g, 0);
+        cudaGraphDestroy(g);
+      } else if (e == cudaSuccess) {
+        cudaGraphDestroy(g);
+        e = le;
+      }
+    }
+    if (e != cudaSuccess || !B->graph) {
+      // capture of cooperative launches unavailable: launch directly
+      cudaGetLastError();
+      B->use_graph = false;
+      B->graph = nullptr;
+    } else {
+      B->graph_steps = nsteps;
+    }
+  }
+  if (B->use_graph) {
+    e = cudaGraphLaunch(B->graph, B->stream);
+    if (e != cudaSuccess) return B->cuda_fail(e, "cudaGraphLaunch");
+  } else {
+    e = cudaMemsetAsync(B->d_bar, 0, sizeof(GridBarrier), B->stream);
+    if (e == cudaSuccess) e = B->ks->persistent(B->d, B->plan, grid, B->block, B->stream);
+    if (e != cudaSuccess) return B->cuda_fail(e, "persistent launch");
+  }
+  return FVS_OK;
+}
+
+int check_barrier(fvs_batch* B) {
+  GridBarrier gb;
+  cudaError_t e = cudaMemcpyAsync(&gb, B->d_bar, sizeof gb, cudaMemcpyDeviceToHost, B->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(B->stream);
+  if (e != cudaSuccess) return B->cuda_fail(e, "persistent kernel");
+  if (gb.err) return B->fail(FVS_ERR_TIMEOUT, "a grid barrier of the persistent kernel ran out of its wait budget");
+  return FVS_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int fvs_batch_create(const fvs_mesh* meshes, const fvs_options* opts, int32_t ncases, int32_t host_threads,
+                     fvs_batch** out) {
+  if (!out) return FVS_ERR_INVALID;
+  *out = nullptr;
+  if (!meshes || !opts || ncases <= 0) {
+    g_batch_create_error = "invalid batch description";
+    return FVS_ERR_INVALID;
+  }
+  const fvs_options& o0 = opts[0];
+  for (int c = 1; c < ncases; c++)
+    if (!same_scheme(o0, opts[c])) {
+      g_batch_create_error = "case " + std::to_string(c) + ": all cases of a batch share the scheme (only Mach and angle of attack differ)";
+      return FVS_ERR_INVALID;
+    }
+  if (o0.grad_method != FVS_GRAD_LSQ || o0.dt_from_cfl || o0.flux != 1 || o0.rk_nstages < 3 || o0.rk_nstages > 4) {
+    g_batch_create_error = "batches run LSQ gradients with a fixed dt (or steady)";
+    return FVS_ERR_INVALID;
+  }
+  std::unique_ptr<fvs_batch> B(new fvs_batch());
+  B->ncases = ncases;
+  B->opt.assign(opts, opts + ncases);
+  B->base = o0;
+  if (B->base.reconst != FVS_RECON_UMUSCL) B->base.umuscl = 0.0;
+  B->hm.resize(ncases);
+  // host preprocessing of the cases in parallel
+  std::vector<std::string> errs(ncases);
+  std::vector<int> rcs(ncases, 0);
+  std::atomic<int> next(0);
+  int nth = host_threads > 0 ? host_threads : (int)std::max(1u, std::thread::hardware_concurrency());
+  nth = std::min(nth, ncases);
+  std::vector<std::thread> pool;
+  for (int t = 0; t < nth; t++)
+    pool.emplace_back([&]() {
+      for (int c = next++; c < ncases; c = next++) {
+        fvs_options oc = opts[c];
+        if (oc.reconst != FVS_RECON_UMUSCL) oc.umuscl = 0.0;
+        rcs[c] = build_host_mesh(&meshes[c], &oc, B->hm[c], errs[c]);
+      }
+    });
+  for (auto& th : pool) th.join();
+  for (int c = 0; c < ncases; c++)
+    if (rcs[c]) {
+      g_batch_create_error = "case " + std::to_string(c) + ": " + errs[c];
+      return rcs[c];
+    }
+  B->pinf.resize(4 * (size_t)ncases);
+  for (int c = 0; c < ncases; c++) {
+    const double aoa = opts[c].aoa_inf_deg * 3.141592653589793238462643383279502884 / 180.0;
+    B->pinf[4 * c] = 1.0;
+    B->pinf[4 * c + 1] = opts[c].mach_inf * std::cos(aoa);
+    B->pinf[4 * c + 2] = opts[c].mach_inf * std::sin(aoa);
+    B->pinf[4 * c + 3] = 1.0 / opts[c].gamma;
+  }
+  B->mixed = o0.precision == FVS_PREC_MIXED;
+  B->ks = B->mixed ? &kernels_mixed()
+          : (o0.precision == FVS_PREC_FP64_STRICT ? &kernels_fp64_strict() : &kernels_fp64_fast());
+  cudaError_t e = cudaStreamCreateWithFlags(&B->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) { g_batch_create_error = std::string("cudaStreamCreate: ") + cudaGetErrorString(e); return FVS_ERR_CUDA; }
+  cudaMallocHost(&B->h_step0, 16);
+  cudaEventCreate(&B->ev0);
+  cudaEventCreate(&B->ev1);
+  cudaDeviceGetAttribute(&B->nsm, cudaDevAttrMultiProcessorCount, 0);
+  DevView& d = B->d;
+  const fvs_options& ob = B->base;
+  d.gamma = ob.gamma; d.gm1 = ob.gamma - 1.0; d.igm1 = 1.0 / (ob.gamma - 1.0);
+  d.khalf = ob.umuscl / 2.0; d.nkhalf = -ob.umuscl / 2.0; d.omk = 1.0 - ob.umuscl; d.cfl = ob.cfl;
+  d.fgamma = float(d.gamma); d.fgm1 = float(d.gm1); d.figm1 = float(d.igm1);
+  d.fkhalf = float(d.khalf); d.fnkhalf = float(d.nkhalf); d.fomk = float(d.omk);
+  d.limiter = ob.limiter; d.grad_method = ob.grad_method; d.first_order = ob.reconst == FVS_RECON_UPWIND1;
+  d.vortex = ob.vortex; d.vx = ob.vortex_x; d.vy = ob.vortex_y; d.vkappa = ob.vortex_kappa;
+  for (int k = 0; k < 4; k++) { d.vinf[k] = ob.vortex_inf[k]; d.pinf[k] = B->pinf[k]; }
+  mms_constants(d.mc);
+  int rc = B->mixed ? build_batch_device<float>(B.get()) : build_batch_device<double>(B.get());
+  if (rc) { g_batch_create_error = B->err; return rc; }
+  set_batch_stages(B.get());
+  B->active.assign(ncases, 1);
+  if (B->ks->persistent_occupancy(B->d, B->block) <= 0) {
+    g_batch_create_error = "no persistent kernel for this scheme";
+    return FVS_ERR_INVALID;
+  }
+  e = cudaDeviceSynchronize();
+  if (e != cudaSuccess) { g_batch_create_error = std::string("batch setup: ") + cudaGetErrorString(e); return FVS_ERR_CUDA; }
+  *out = B.release();
+  return FVS_OK;
+}
+
+void fvs_batch_destroy(fvs_batch* b) { delete b; }
+
+const char* fvs_batch_last_error(const fvs_batch* b) { return b ? b->err.c_str() : g_batch_create_error.c_str(); }
+
+int fvs_batch_info(const fvs_batch* b, int32_t* ncells, int32_t* nedges, int32_t* launch4) {
+  if (!b) return FVS_ERR_INVALID;
+  if (ncells) *ncells = b->nc;
+  if (nedges) *nedges = b->ne;
+  if (launch4) {
+    launch4[0] = b->block;
+    launch4[1] = b->tile;
+    launch4[2] = b->bps;
+    launch4[3] = b->use_graph ? 1 : 0;
+  }
+  return FVS_OK;
+}
+
+int fvs_batch_set_state(fvs_batch* b, int32_t icase, const double* cvar) {
+  if (!b || !cvar || icase < 0 || icase >= b->ncases) return FVS_ERR_INVALID;
+  const int n = b->cnum[icase];
+  cudaError_t e = cudaMemcpyAsync(b->d_stage, cvar, 32 * (size_t)n, cudaMemcpyHostToDevice, b->stream);
+  if (e != cudaSuccess) return b->cuda_fail(e, "state upload");
+  kb_scatter_in<<<(n + 255) / 256, 256, 0, b->stream>>>(b->d_stage, b->d_perm + b->ref_off[icase], b->d.U, n);
+  // primitives with the kernel set's own conversion (the same rounding as
+  // the update kernel produces them)
+  b->ks->cvar2pvar(b->d, b->stream);
+  e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+  return e == cudaSuccess ? FVS_OK : b->cuda_fail(e, "set_state");
+}
+
+int fvs_batch_get_state(fvs_batch* b, int32_t icase, double* cvar) {
+  if (!b || !cvar || icase < 0 || icase >= b->ncases) return FVS_ERR_INVALID;
+  const int n = b->cnum[icase];
+  kb_gather_out<<<(n + 255) / 256, 256, 0, b->stream>>>(b->d.U, b->d_perm + b->ref_off[icase], b->d_stage, n);
+  cudaError_t e = cudaMemcpyAsync(cvar, b->d_stage, 32 * (size_t)n, cudaMemcpyDeviceToHost, b->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+  return e == cudaSuccess ? FVS_OK : b->cuda_fail(e, "get_state");
+}
+
+int fvs_batch_init_state(fvs_batch* b) {
+  if (!b) return FVS_ERR_INVALID;
+  // free stream of each case (src/initialize.f90:36-44)
+  for (int c = 0; c < b->ncases; c++) {
+    const double* p = &b->pinf[4 * c];
+    const double g = b->opt[c].gamma;
+    double u[4] = {p[0], p[0] * p[1], p[0] * p[2], p[3] / (g - 1.0) + 0.5 * p[0] * (p[1] * p[1] + p[2] * p[2])};
+    std::vector<double> cv(4 * (size_t)b->cnum[c]);
+    for (int i = 0; i < b->cnum[c]; i++) std::memcpy(&cv[4 * i], u, sizeof u);
+    int rc = fvs_batch_set_state(b, c, cv.data());
+    if (rc) return rc;
+  }
+  return FVS_OK;
+}
+
+int fvs_batch_set_barrier_budget(fvs_batch* b, double seconds) {
+  if (!b || seconds < 0) return FVS_ERR_INVALID;
+  b->budget_s = seconds;
+  b->plan_dirty = true;
+  return FVS_OK;
+}
+
+int fvs_batch_set_launch(fvs_batch* b, int32_t block, int32_t tile, int32_t blocks_per_sm) {
+  if (!b || (block != 64 && block != 128 && block != 256) || tile < block || blocks_per_sm < 1) return FVS_ERR_INVALID;
+  if (b->ks->persistent_occupancy(b->d, block) <= 0) return b->fail(FVS_ERR_INVALID, "block size does not fit");
+  b->block = block;
+  b->tile = tile;
+  b->bps = blocks_per_sm;
+  b->plan_dirty = true;
+  return FVS_OK;
+}
+
+// nsteps steps of every active case; norms (optional) [ncases][nsteps][4]
+int fvs_batch_steps(fvs_batch* b, int32_t nsteps, double* norms, float* ms) {
+  if (!b || nsteps <= 0 || nsteps > b->norm_cap) return FVS_ERR_INVALID;
+  cudaEventRecord(b->ev0, b->stream);
+  int rc = launch_chunk(b, nsteps, 0);
+  if (rc) return rc;
+  cudaEventRecord(b->ev1, b->stream);
+  if ((rc = check_barrier(b))) return rc;
+  if (ms) cudaEventElapsedTime(ms, b->ev0, b->ev1);
+  if (norms) {
+    std::vector<double> all(4 * (size_t)b->ncases * b->norm_cap);
+    cudaError_t e = cudaMemcpy(all.data(), b->d_case_norms, 8 * all.size(), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return b->cuda_fail(e, "norm download");
+    for (int c = 0; c < b->ncases; c++)
+      std::memcpy(norms + 4 * (size_t)c * nsteps, &all[4 * (size_t)c * b->norm_cap], 32 * (size_t)nsteps);
+  }
+  return FVS_OK;
+}
+
+// Candidate launch shapes timed on the batch itself; the state is restored.
+int fvs_batch_autotune(fvs_batch* b, int32_t trial_steps, float* best_ms) {
+  if (!b || trial_steps <= 0 || trial_steps > b->norm_cap) return FVS_ERR_INVALID;
+  cudaError_t e = cudaMemcpy(b->d_backup, b->d.U, 32 * (size_t)b->nc, cudaMemcpyDeviceToDevice);
+  if (e != cudaSuccess) return b->cuda_fail(e, "state backup");
+  const int blocks[2] = {128, 256};
+  const int tiles_per_block[3] = {1, 4, 16};
+  float best = 1e30f;
+  int bb = b->block, bt = b->tile, bp = b->bps;
+  for (int blk : blocks) {
+    const int occ = b->ks->persistent_occupancy(b->d, blk);
+    if (occ <= 0) continue;
+    const int bps_list[3] = {1, std::max(1, occ / 2), occ};
+    for (int tpb : tiles_per_block)
+      for (int q = 0; q < 3; q++) {
+        if (q > 0 && bps_list[q] == bps_list[q - 1]) continue;
+        b->block = blk;
+        b->tile = blk * tpb;
+        b->bps = bps_list[q];
+        b->plan_dirty = true;
+        float ms = 0.f;
+        int rc = fvs_batch_steps(b, 1, nullptr, nullptr);  // warm-up, graph capture
+        if (!rc) rc = fvs_batch_steps(b, trial_steps, nullptr, &ms);
+        if (rc) return rc;
+        if (ms < best) {
+          best = ms;
+          bb = blk; bt = blk * tpb; bp = bps_list[q];
+        }
+      }
+  }
+  b->block = bb;
+  b->tile = bt;
+  b->bps = bp;
+  b->plan_dirty = true;
+  e = cudaMemcpy(b->d.U, b->d_backup, 32 * (size_t)b->nc, cudaMemcpyDeviceToDevice);
+  if (e != cudaSuccess) return b->cuda_fail(e, "state restore");
+  // primitives of the restored state
+  b->ks->cvar2pvar(b->d, b->stream);
+  e = cudaStreamSynchronize(b->stream);
+  if (e != cudaSuccess) return b->cuda_fail(e, "autotune restore");
+  if (best_ms) *best_ms = best / trial_steps;
+  return FVS_OK;
+}
+
+// Steps all cases until each one's RMS(dU_rho) falls to drop x its first
+// value (or max_steps).  steps_done[c] = the step at which case c reached the
+// drop (max_steps if it did not); first/last [ncases][4] norms.
+int fvs_batch_run_to_drop(fvs_batch* b, int32_t max_steps, double drop, int32_t chunk, int32_t* steps_done,
+                          double* first, double* last, float* ms) {
+  if (!b || max_steps <= 0 || chunk <= 0 || chunk > b->norm_cap) return FVS_ERR_INVALID;
+  const int nc = b->ncases;
+  std::vector<double> f(4 * (size_t)nc, -1.0), l(4 * (size_t)nc, 0.0);
+  std::vector<int> done(nc, max_steps);
+  std::fill(b->active.begin(), b->active.end(), 1);
+  b->plan_dirty = true;
+  std::vector<double> all(4 * (size_t)nc * b->norm_cap);
+  cudaEventRecord(b->ev0, b->stream);
+  int step = 0, rc = FVS_OK;
+  bool nonfinite = false;
+  while (step < max_steps) {
+    const int n = std::min(chunk, max_steps - step);
+    if ((rc = launch_chunk(b, n, step))) break;
+    if ((rc = check_barrier(b))) break;
+    cudaError_t e = cudaMemcpy(all.data(), b->d_case_norms, 8 * all.size(), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) { rc = b->cuda_fail(e, "norm download"); break; }
+    bool changed = false;
+    int nact = 0;
+    for (int c = 0; c < nc; c++) {
+      if (!b->active[c]) continue;
+      for (int s = 0; s < n; s++) {
+        const double* v = &all[4 * ((size_t)c * b->norm_cap + (step + s) % b->norm_cap)];
+        if (!std::isfinite(v[0])) { nonfinite = true; b->active[c] = 0; done[c] = step + s + 1; changed = true; break; }
+        if (f[4 * c] < 0) std::memcpy(&f[4 * c], v, 32);
+        std::memcpy(&l[4 * c], v, 32);
+        if (v[0] <= drop * f[4 * c]) {
+          done[c] = step + s + 1;
+          b->active[c] = 0;
+          changed = true;
+          break;
+        }
+      }
+      nact += b->active[c];
+    }
+    step += n;
+    if (nact == 0) break;
+    if (changed) b->plan_dirty = true;
+  }
+  cudaEventRecord(b->ev1, b->stream);
+  cudaEventSynchronize(b->ev1);
+  if (ms) cudaEventElapsedTime(ms, b->ev0, b->ev1);
+  std::fill(b->active.begin(), b->active.end(), 1);
+  b->plan_dirty = true;
+  if (steps_done) std::memcpy(steps_done, done.data(), 4 * (size_t)nc);
+  if (first) std::memcpy(first, f.data(), 32 * (size_t)nc);
+  if (last) std::memcpy(last, l.data(), 32 * (size_t)nc);
+  if (rc) return rc;
+  return nonfinite ? b->fail(FVS_ERR_NONFINITE, "a case's residual norm is not finite") : FVS_OK;
+}
+
+}  // extern "C"

@@ -16,17 +16,13 @@
 #include <vector>
 
 #include "fvs_internal.hpp"
+#include "fvs_layout.hpp"
 
 using namespace fvs;
 
 namespace {
 
 thread_local std::string g_create_error;
-
-struct DevBuf {
-  void* p = nullptr;
-  size_t n = 0;
-};
 
 __global__ void k_scatter_in(const double* __restrict__ ref, const int* __restrict__ perm, double* __restrict__ dev, int nc) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -61,7 +57,7 @@ struct fvs_handle {
   const KernelSet* ks = nullptr;
   bool mixed = false;
   cudaStream_t stream = nullptr;
-  std::vector<void*> allocs;
+  DeviceArena arena;
   DevView d;
   std::vector<int> perm;   // reference cell -> device cell
   int* d_perm = nullptr;   // device copy of perm
@@ -81,7 +77,7 @@ struct fvs_handle {
     if (graph) cudaGraphExecDestroy(graph);
     if (ev0) cudaEventDestroy(ev0);
     if (ev1) cudaEventDestroy(ev1);
-    for (void* p : allocs) cudaFree(p);
+    arena.release();
     if (h_small) cudaFreeHost(h_small);
     if (stream) cudaStreamDestroy(stream);
   }
@@ -94,263 +90,32 @@ struct fvs_handle {
     err = std::string(where) + ": " + cudaGetErrorString(e);
     return FVS_ERR_CUDA;
   }
-  template <typename V>
-  bool upload(V*& dst, const std::vector<V>& src) {
-    dst = nullptr;
-    if (src.empty()) return true;
-    void* p = nullptr;
-    if (cudaMalloc(&p, sizeof(V) * src.size()) != cudaSuccess) return false;
-    allocs.push_back(p);
-    if (cudaMemcpy(p, src.data(), sizeof(V) * src.size(), cudaMemcpyHostToDevice) != cudaSuccess) return false;
-    dst = static_cast<V*>(p);
-    return true;
-  }
-  bool alloc(void*& dst, size_t bytes) {
-    dst = nullptr;
-    if (bytes == 0) bytes = 16;
-    if (cudaMalloc(&dst, bytes) != cudaSuccess) return false;
-    allocs.push_back(dst);
-    return cudaMemset(dst, 0, bytes) == cudaSuccess;
-  }
 };
 
 namespace {
 
-// reverse Cuthill-McKee over face neighbours: BFS from a pseudo-peripheral
-// cell, neighbours visited by increasing degree, order reversed.
-std::vector<int> rcm_order(const HostMesh& h) {
-  const int nc = h.nc;
-  std::vector<int> deg(nc, 0);
-  for (int ic = 0; ic < nc; ic++)
-    for (int k = 0; k < h.nvrt[ic]; k++) deg[ic] += h.nghbr[4 * ic + k] >= 0;
-  std::vector<int> order;
-  order.reserve(nc);
-  std::vector<char> seen(nc, 0);
-  std::vector<int> level(nc, -1);
-  auto bfs_last = [&](int s) {
-    // farthest cell of minimum degree from s (one sweep)
-    std::vector<int> q{s};
-    std::fill(level.begin(), level.end(), -1);
-    level[s] = 0;
-    for (size_t i = 0; i < q.size(); i++) {
-      int c = q[i];
-      for (int k = 0; k < h.nvrt[c]; k++) {
-        int n = h.nghbr[4 * c + k];
-        if (n >= 0 && level[n] < 0) { level[n] = level[c] + 1; q.push_back(n); }
-      }
-    }
-    int best = q.back();
-    for (int c : q)
-      if (level[c] == level[q.back()] && deg[c] < deg[best]) best = c;
-    return best;
-  };
-  int next_unseen = 0;
-  while ((int)order.size() < nc) {
-    while (seen[next_unseen]) next_unseen++;
-    int start = next_unseen;
-    for (int ic = next_unseen; ic < nc; ic++)
-      if (!seen[ic] && deg[ic] < deg[start]) start = ic;
-    start = bfs_last(bfs_last(start));
-    size_t head = order.size();
-    order.push_back(start);
-    seen[start] = 1;
-    int nb[4];
-    while (head < order.size()) {
-      int c = order[head++];
-      int m = 0;
-      for (int k = 0; k < h.nvrt[c]; k++) {
-        int n = h.nghbr[4 * c + k];
-        if (n >= 0 && !seen[n]) nb[m++] = n;
-      }
-      std::sort(nb, nb + m, [&](int a, int b) { return deg[a] != deg[b] ? deg[a] < deg[b] : a < b; });
-      for (int i = 0; i < m; i++) {
-        seen[nb[i]] = 1;
-        order.push_back(nb[i]);
-      }
-    }
-  }
-  std::reverse(order.begin(), order.end());
-  std::vector<int> perm(nc);
-  for (int i = 0; i < nc; i++) perm[order[i]] = i;
-  return perm;
-}
-
-inline double minimg(double d, double L) { return L > 0 ? d - L * std::nearbyint(d / L) : d; }
-
-template <typename T>
-std::vector<T> conv(const std::vector<double>& v) {
-  return std::vector<T>(v.begin(), v.end());
-}
-
 // Builds every device array of the handle from the host mesh.
 template <typename T>
 int build_device(fvs_handle* H) {
-  HostMesh& h = H->hm;
+  Layout<T> L;
+  std::string err;
+  const bool fold_w = H->o.precision != FVS_PREC_FP64_STRICT;
+  int rc = append_case(L, H->hm, fold_w, 0, err);
+  if (rc) return H->fail(rc, err);
+  H->perm = L.perm;
   DevView& d = H->d;
-  const int nc = h.nc;
-  H->perm = rcm_order(h);
-  const std::vector<int>& perm = H->perm;
-  std::vector<int> iperm(nc);
-  for (int i = 0; i < nc; i++) iperm[perm[i]] = i;
-  const int nint = (int)h.edge_intr.size(), nbe = (int)h.b_edge.size();
-  d.nc = nc;
-  d.nint = nint;
-  d.nedge = nint + nbe;
-  // interior edge slots sorted by their first device cell (stable)
-  std::vector<int> eorder(nint);
-  std::iota(eorder.begin(), eorder.end(), 0);
-  std::stable_sort(eorder.begin(), eorder.end(), [&](int a, int b) {
-    int ea = h.edge_intr[a], eb = h.edge_intr[b];
-    int ka = std::min(perm[h.ec1[ea]], perm[h.ec2[ea]]), kb = std::min(perm[h.ec1[eb]], perm[h.ec2[eb]]);
-    return ka < kb;
-  });
-  std::vector<int> slot_of_intr(nint);
-  for (int s = 0; s < nint; s++) slot_of_intr[eorder[s]] = s;
-  const int ne = d.nedge;
-  std::vector<int2> ecell(ne);
-  std::vector<T> enrm(2 * (size_t)ne), earea(ne), edL(2 * (size_t)ne), edR(2 * (size_t)std::max(nint, 1));
-  std::vector<int> ebtype(std::max(nbe, 1));
-  std::vector<T> exy(2 * (size_t)std::max(nbe, 1));
-  for (int s = 0; s < nint; s++) {
-    int ie = h.edge_intr[eorder[s]];
-    int L = h.ec1[ie], R = h.ec2[ie];
-    ecell[s] = make_int2(perm[L], perm[R]);
-    enrm[2 * s] = T(h.enx[ie]); enrm[2 * s + 1] = T(h.eny[ie]);
-    earea[s] = T(h.ea[ie]);
-    edL[2 * s] = T(minimg(h.ex[ie] - h.xc[L], h.Lx)); edL[2 * s + 1] = T(minimg(h.ey[ie] - h.yc[L], h.Ly));
-    edR[2 * s] = T(minimg(h.ex[ie] - h.xc[R], h.Lx)); edR[2 * s + 1] = T(minimg(h.ey[ie] - h.yc[R], h.Ly));
-  }
-  // boundary edges in the reference's processing order; edge i of boundary
-  // ib is paired with bndry(ib)%cell(i) (src/residual.f90:114-125)
-  std::vector<int> bcell_of(nbe);
-  for (int ib = 0, k = 0; ib < h.nb; ib++)
-    for (int i = h.b_eptr[ib]; i < h.b_eptr[ib + 1]; i++, k++) {
-      int ie = h.b_edge[i], L = h.b_cell[h.b_cptr[ib] + (i - h.b_eptr[ib])], s = nint + k;
-      bcell_of[k] = L;
-      ecell[s] = make_int2(perm[L], -1);
-      enrm[2 * s] = T(h.enx[ie]); enrm[2 * s + 1] = T(h.eny[ie]);
-      earea[s] = T(h.ea[ie]);
-      edL[2 * s] = T(minimg(h.ex[ie] - h.xc[L], h.Lx)); edL[2 * s + 1] = T(minimg(h.ey[ie] - h.yc[L], h.Ly));
-      ebtype[k] = h.b_type[ib];
-      exy[2 * k] = T(h.ex[ie]); exy[2 * k + 1] = T(h.ey[ie]);
-    }
-  // gather lists in the reference's summation order: interior edges in
-  // edge_intr order (+ to c1, - to c2), then boundary edges
-  std::vector<int4> cf(nc, make_int4(0, 0, 0, 0));
-  std::vector<int> ncf(nc, 0);
-  auto push = [&](int cell, int v) -> bool {
-    int dc = perm[cell];
-    if (ncf[dc] >= 4) return false;
-    int* p = reinterpret_cast<int*>(&cf[dc]);
-    p[ncf[dc]++] = v;
-    return true;
-  };
-  for (int i = 0; i < nint; i++) {
-    int ie = h.edge_intr[i], s = slot_of_intr[i];
-    if (!push(h.ec1[ie], s + 1) || !push(h.ec2[ie], -(s + 1))) return H->fail(FVS_ERR_MESH, "a cell has more than 4 flux contributions");
-  }
-  for (int k = 0; k < nbe; k++)
-    if (!push(bcell_of[k], nint + k + 1)) return H->fail(FVS_ERR_MESH, "a cell has more than 4 flux contributions");
-  // cell arrays in device order
-  std::vector<double> vol(nc), rvol(nc);
-  std::vector<T> eps2(nc), cpos(8 * (size_t)nc, T(0)), rvolT(nc);
-  std::vector<int8_t> nvrt(nc);
-  for (int o = 0; o < nc; o++) {
-    int dc = perm[o];
-    vol[dc] = h.vol[o];
-    rvol[dc] = 1.0 / h.vol[o];
-    rvolT[dc] = T(1.0 / h.vol[o]);
-    eps2[dc] = T(h.eps2[o]);
-    nvrt[dc] = h.nvrt[o];
-    for (int k = 0; k < h.nvrt[o]; k++) {
-      int je = h.cedge[4 * o + k];
-      cpos[8 * dc + 2 * k] = T(minimg(h.ex[je] - h.xc[o], h.Lx));
-      cpos[8 * dc + 2 * k + 1] = T(minimg(h.ey[je] - h.yc[o], h.Ly));
-    }
-  }
-  // stencils in device order, per-cell entry order kept
-  std::vector<int> st_ptr(nc + 1, 0), st_cell;
-  std::vector<T> st_coef, st_w, coef0, coefedg;
-  std::vector<int8_t> st_node;
-  const bool ggnb = h.grad_method == FVS_GRAD_GGNB;
-  const bool fold_w = h.grad_method == FVS_GRAD_LSQ && H->o.precision != FVS_PREC_FP64_STRICT;
-  for (int dc = 0; dc < nc; dc++) {
-    int o = iperm[dc];
-    for (int k = h.st_ptr[o]; k < h.st_ptr[o + 1]; k++) {
-      st_cell.push_back(perm[h.st_cell[k]]);
-      if (ggnb) {
-        st_coef.push_back(T(h.st_coef[k]));
-        st_node.push_back(h.st_node[k]);
-      } else if (fold_w) {
-        // FP64 / MIXED: the LSQ weight folded into the coefficients (setup in FP64)
-        st_coef.push_back(T(h.st_coef[2 * k] * h.st_w[k]));
-        st_coef.push_back(T(h.st_coef[2 * k + 1] * h.st_w[k]));
-      } else {
-        st_coef.push_back(T(h.st_coef[2 * k]));
-        st_coef.push_back(T(h.st_coef[2 * k + 1]));
-      }
-      if (!h.st_w.empty()) st_w.push_back(T(h.st_w[k]));
-    }
-    st_ptr[dc + 1] = (int)st_cell.size();
-  }
-  if (!h.coef0.empty()) {
-    coef0.resize(2 * (size_t)nc);
-    for (int o = 0; o < nc; o++) { coef0[2 * perm[o]] = T(h.coef0[2 * o]); coef0[2 * perm[o] + 1] = T(h.coef0[2 * o + 1]); }
-  }
-  if (!h.coefedg.empty()) {
-    coefedg.resize(8 * (size_t)nc);
-    for (int o = 0; o < nc; o++)
-      for (int k = 0; k < 8; k++) coefedg[8 * perm[o] + k] = T(h.coefedg[8 * o + k]);
-  }
-  // upload
-  bool ok = true;
-  double *dvol, *drvol;
-  int4* dcf;
-  int8_t *dnv, *dsn;
-  int *dsp, *dsc, *deb, *dperm;
-  int2* dec;
-  T *t_rvol, *t_eps2, *t_cpos, *t_coef, *t_w, *t_c0, *t_ce, *t_nrm, *t_area, *t_edL, *t_edR, *t_exy;
-  ok = ok && H->upload(dvol, vol) && H->upload(drvol, rvol) && H->upload(dcf, cf) && H->upload(dnv, nvrt);
-  ok = ok && H->upload(dsp, st_ptr) && H->upload(dsc, st_cell) && H->upload(dsn, st_node) && H->upload(dec, ecell);
-  ok = ok && H->upload(deb, ebtype) && H->upload(dperm, perm);
-  ok = ok && H->upload(t_rvol, rvolT) && H->upload(t_eps2, eps2) && H->upload(t_cpos, cpos) && H->upload(t_coef, st_coef) && H->upload(t_w, st_w);
-  ok = ok && H->upload(t_c0, coef0) && H->upload(t_ce, coefedg) && H->upload(t_nrm, enrm) && H->upload(t_area, earea);
-  ok = ok && H->upload(t_edL, edL) && H->upload(t_edR, edR) && H->upload(t_exy, exy);
+  int* dperm = nullptr;
+  if (!upload_layout(H->arena, L, d) || !H->arena.upload(dperm, L.perm))
+    return H->fail(FVS_ERR_NOMEM, "device allocation or upload of the mesh failed");
   H->d_perm = dperm;
-  if (!ok) return H->fail(FVS_ERR_NOMEM, "device allocation or upload of the mesh failed");
-  d.vol = dvol; d.rvol = drvol; d.cflist = dcf; d.nvrt = dnv; d.st_ptr = dsp; d.st_cell = dsc; d.st_node = dsn;
-  d.ecell = dec; d.ebtype = deb; d.volT = t_rvol; d.eps2 = t_eps2; d.cpos = t_cpos; d.st_coef = t_coef; d.st_w = t_w; d.coef0 = t_c0;
-  d.coefedg = t_ce; d.enrm = t_nrm; d.earea = t_area; d.edL = t_edL; d.edR = t_edR; d.exy = t_exy;
-  // state and work arrays
+  H->nblk = (L.nc + 255) / 256;
   void* p;
-  const size_t n4 = 4 * (size_t)nc;
-  H->nblk = (nc + 255) / 256;
-  d.nblk_red = H->nblk;
-  d.norm_cap = 4096;
-#define FVS_ALLOC(field, type, bytes) ok = ok && H->alloc(p, bytes); d.field = static_cast<type>(p)
-  FVS_ALLOC(U, double*, 8 * n4);
-  FVS_ALLOC(U0, double*, 8 * n4);
-  FVS_ALLOC(F, double*, 8 * n4);
-  FVS_ALLOC(resid, double*, 8 * n4);
-  FVS_ALLOC(ws, double*, 8 * (size_t)nc);
-  FVS_ALLOC(dtl, double*, 8 * (size_t)nc);
-  FVS_ALLOC(Pv, void*, sizeof(T) * n4);
-  FVS_ALLOC(Gx, void*, sizeof(T) * n4);
-  FVS_ALLOC(Gy, void*, sizeof(T) * n4);
-  FVS_ALLOC(phi, void*, sizeof(T) * (size_t)nc);
-  FVS_ALLOC(eflux, void*, sizeof(T) * 4 * (size_t)ne);
-  FVS_ALLOC(ews, void*, sizeof(T) * (size_t)ne);
-  FVS_ALLOC(partials, double*, 32 * (size_t)H->nblk);
-  FVS_ALLOC(norms, double*, 32 * (size_t)d.norm_cap);
-  FVS_ALLOC(stepctl, int*, 16);
-  FVS_ALLOC(tctl, double*, 16);
-#undef FVS_ALLOC
-  ok = ok && H->alloc(p, 8 * n4);
+  if (!alloc_work<T>(H->arena, d, L.nc, L.ne, H->nblk, 4096) || !H->arena.alloc(p, 32 * (size_t)L.nc))
+    return H->fail(FVS_ERR_NOMEM, "device allocation of the state failed");
   H->d_stage = static_cast<double*>(p);
-  if (!ok) return H->fail(FVS_ERR_NOMEM, "device allocation of the state failed");
   // phi: 0 for first order, 1 without a limiter (src/gradient_limiter.f90:30-40)
-  std::vector<T> phi0(nc, T(H->o.reconst == FVS_RECON_UPWIND1 ? 0.0 : 1.0));
-  if (cudaMemcpy(d.phi, phi0.data(), sizeof(T) * nc, cudaMemcpyHostToDevice) != cudaSuccess)
+  std::vector<T> phi0(L.nc, T(H->o.reconst == FVS_RECON_UPWIND1 ? 0.0 : 1.0));
+  if (cudaMemcpy(d.phi, phi0.data(), sizeof(T) * L.nc, cudaMemcpyHostToDevice) != cudaSuccess)
     return H->fail(FVS_ERR_CUDA, "phi upload failed");
   return FVS_OK;
 }

@@ -108,8 +108,9 @@ struct DevView {
   const void* earea = nullptr;    // [nedge] (T)
   const void* edL = nullptr;      // [nedge] x 2 xf - xcL (T)
   const void* edR = nullptr;      // [nint] x 2 xf - xcR (T)
-  const int* ebtype = nullptr;    // [nedge-nint] boundary type
-  const void* exy = nullptr;      // [nedge-nint] x 2 face centre (T)
+  const int* ebtype = nullptr;    // [nedge] boundary record: type | case << 4 (boundary slots only)
+  const void* exy = nullptr;      // [nedge] x 2 face centre (T) (boundary slots only)
+  const double* case_pinf = nullptr;  // [ncases][4] free stream per case (batched meshes)
   void* eflux = nullptr;          // [nedge] x 4 flux*area (T)
   void* ews = nullptr;            // [nedge] ws_max*area (T)
   // reduction and step control
@@ -139,6 +140,38 @@ struct StageParams {
   double dts = 0;     // stage time offset from told
 };
 
+// Software grid barrier of the persistent kernel.  Every wait is bounded by a
+// clock64() budget; a wait that runs out sets err, every block leaves at its
+// next barrier and the host reports FVS_ERR_TIMEOUT.
+struct GridBarrier {
+  unsigned int count;
+  unsigned int gen;
+  int err;
+  int pad;
+};
+
+// Work plan of the persistent kernel: nsteps RK steps over tile lists.
+// Cell tiles never straddle two cases, so each tile's partial norm belongs
+// to one case.  Only the tiles of active (not yet converged) cases are listed.
+struct PersistPlan {
+  int nsteps = 1, nstages = 4;
+  StageParams sp[4];
+  double t1 = 0;
+  const int* step0_dev = nullptr;        // device word: global index of the launch's first step;
+                                         // told = t1 + (step0 + s) * dt
+  const int4* cell_tiles = nullptr;      // x = first cell, y = end, z = case
+  int ncell_tiles = 0;
+  const int2* edge_tiles = nullptr;      // x = first edge slot, y = end
+  int nedge_tiles = 0;
+  const int4* case_tiles = nullptr;      // x = case, y = first cell tile, z = end tile, w = cells of the case
+  int ncase_active = 0;
+  double* tile_partials = nullptr;       // [ncell_tiles][4]
+  double* case_norms = nullptr;          // [ncases][norm_cap][4]
+  int norm_cap = 0;
+  GridBarrier* bar = nullptr;
+  long long budget = 0;                  // clock64 cycles one barrier wait may take
+};
+
 // Kernel launchers, one set per arithmetic variant (strict FP64, FP64 with
 // FMA, mixed).  All launch on the given stream; none synchronises.
 struct KernelSet {
@@ -150,6 +183,10 @@ struct KernelSet {
   void (*update)(const DevView&, const StageParams&, cudaStream_t);
   void (*residual_out)(const DevView&, cudaStream_t);
   void (*norm_final)(const DevView&, cudaStream_t);
+  // persistent kernel (LSQ gradients): resident blocks per SM for a block
+  // size (0: the scheme has no persistent variant), and the cooperative launch
+  int (*persistent_occupancy)(const DevView&, int block);
+  cudaError_t (*persistent)(const DevView&, const PersistPlan&, int grid, int block, cudaStream_t);
 };
 const KernelSet& kernels_fp64_strict();
 const KernelSet& kernels_fp64_fast();

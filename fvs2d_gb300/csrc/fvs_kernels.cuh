@@ -53,6 +53,28 @@ __device__ __forceinline__ T2 ld2(const void* p, int i) {
   return reinterpret_cast<const T2*>(p)[i];
 }
 
+// Loads of arrays that another block wrote earlier in the same launch (the
+// persistent kernel): COH selects ld.global.cg, which reads through L2 and
+// never returns a stale L1 line or a non-coherent read-only-path value.
+template <bool COH>
+__device__ __forceinline__ void ldc4(const double* p, int i, double* o) {
+  const double2* q = reinterpret_cast<const double2*>(p) + 2 * (size_t)i;
+  double2 a, b;
+  if (COH) { a = __ldcg(q); b = __ldcg(q + 1); }
+  else { a = q[0]; b = q[1]; }
+  o[0] = a.x; o[1] = a.y; o[2] = b.x; o[3] = b.y;
+}
+template <bool COH>
+__device__ __forceinline__ void ldc4(const float* p, int i, float* o) {
+  const float4* q = reinterpret_cast<const float4*>(p) + i;
+  const float4 a = COH ? __ldcg(q) : *q;
+  o[0] = a.x; o[1] = a.y; o[2] = a.z; o[3] = a.w;
+}
+template <bool COH, typename V>
+__device__ __forceinline__ V ldc1(const V* p, int i) {
+  return COH ? __ldcg(p + i) : p[i];
+}
+
 // scheme constants in the compute type, rounded once on the host
 #if FVS_MIXED
 #define TP(name) (d.f##name)
@@ -216,13 +238,11 @@ __device__ __forceinline__ void roe_flux_fast(T gamma, T gm1, T igm1, const T* p
 // ---------------------------------------------------------------------------
 // gradient (+ limiter) : one thread per cell
 // ---------------------------------------------------------------------------
-template <int METHOD, int LIM>
-__global__ void __launch_bounds__(256) k_gradient(const DevView d) {
-  const int ic = blockIdx.x * blockDim.x + threadIdx.x;
-  if (ic >= d.nc) return;
-  const T* __restrict__ P = static_cast<const T*>(d.Pv);
+template <int METHOD, int LIM, bool COH>
+__device__ __forceinline__ void gradient_item(const DevView& d, int ic) {
+  const T* P = static_cast<const T*>(d.Pv);
   T pc[4], gx[4], gy[4], pmin[4], pmax[4];
-  ld4(P, ic, pc);
+  ldc4<COH>(P, ic, pc);
 #pragma unroll
   for (int v = 0; v < 4; v++) { pmin[v] = pc[v]; pmax[v] = pc[v]; }
   const int b = d.st_ptr[ic], e = d.st_ptr[ic + 1];
@@ -237,7 +257,7 @@ __global__ void __launch_bounds__(256) k_gradient(const DevView d) {
     for (int k = b; k < e; k++) {
       const int jc = d.st_cell[k];
       T pj[4];
-      ld4(P, jc, pj);
+      ldc4<COH>(P, jc, pj);
       const T2 c = ld2(d.st_coef, k);
 #if FVS_STRICT
       const T w = W[k];
@@ -266,7 +286,7 @@ __global__ void __launch_bounds__(256) k_gradient(const DevView d) {
     for (int v = 0; v < 4; v++) { gx[v] = c0.x * pc[v]; gy[v] = c0.y * pc[v]; }
     for (int k = b; k < e; k++) {
       T pj[4];
-      ld4(P, d.st_cell[k], pj);
+      ldc4<COH>(P, d.st_cell[k], pj);
       const T2 c = ld2(d.st_coef, k);
 #pragma unroll
       for (int v = 0; v < 4; v++) { gx[v] = gx[v] + c.x * pj[v]; gy[v] = gy[v] + c.y * pj[v]; }
@@ -288,7 +308,7 @@ __global__ void __launch_bounds__(256) k_gradient(const DevView d) {
     const T* __restrict__ CN = static_cast<const T*>(d.st_coef);
     for (int k = b; k < e; k++) {
       T pj[4];
-      ld4(P, d.st_cell[k], pj);
+      ldc4<COH>(P, d.st_cell[k], pj);
       const T cn = CN[k];
       const T2 ce = ld2(d.coefedg, 4 * ic + d.st_node[k]);
 #pragma unroll
@@ -336,6 +356,12 @@ __global__ void __launch_bounds__(256) k_gradient(const DevView d) {
   }
 }
 
+template <int METHOD, int LIM>
+__global__ void __launch_bounds__(256) k_gradient(const DevView d) {
+  const int ic = blockIdx.x * blockDim.x + threadIdx.x;
+  if (ic < d.nc) gradient_item<METHOD, LIM, false>(d, ic);
+}
+
 // ---------------------------------------------------------------------------
 // boundary ghost state, bc_flux src/residual.f90:183-255
 // ---------------------------------------------------------------------------
@@ -348,11 +374,14 @@ __device__ __forceinline__ float tsin_(float x) { return sinf(x); }
 __device__ __forceinline__ double tcos_(double x) { return cos(x); }
 __device__ __forceinline__ float tcos_(float x) { return cosf(x); }
 
-__device__ __forceinline__ void ghost_state(const DevView& d, int type, double time, T x, T y, T nx, T ny,
+__device__ __forceinline__ void ghost_state(const DevView& d, int rec, double time, T x, T y, T nx, T ny,
                                             const T* pfL, T* pfR) {
+  const int type = rec & 15;
   if (type == FVS_BC_FREESTREAM) {
+    // the free stream of the slot's case (batched meshes), else the handle's
+    const double* pi = d.case_pinf ? d.case_pinf + 4 * (rec >> 4) : d.pinf;
 #pragma unroll
-    for (int k = 0; k < 4; k++) pfR[k] = T(d.pinf[k]);
+    for (int k = 0; k < 4; k++) pfR[k] = T(pi[k]);
   } else if (type == FVS_BC_SLIP_WALL) {
     const T un = pfL[1] * nx + pfL[2] * ny;
     pfR[0] = pfL[0];
@@ -386,29 +415,27 @@ __device__ __forceinline__ void ghost_state(const DevView& d, int type, double t
 // ---------------------------------------------------------------------------
 // SPEC: non-strict builds only, kappa = 0 and no limiter (phi = 1), where the
 // reconstruction reduces to p + (dx, dy).grad exactly
-template <bool SPEC>
-__global__ void __launch_bounds__(256) k_flux(const DevView d, double dts) {
-  const int e = blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= d.nedge) return;
-  const T* __restrict__ P = static_cast<const T*>(d.Pv);
-  const T* __restrict__ GX = static_cast<const T*>(d.Gx);
-  const T* __restrict__ GY = static_cast<const T*>(d.Gy);
-  const T* __restrict__ PH = static_cast<const T*>(d.phi);
+template <bool SPEC, bool COH>
+__device__ __forceinline__ void flux_item(const DevView& d, int e, double time) {
+  const T* P = static_cast<const T*>(d.Pv);
+  const T* GX = static_cast<const T*>(d.Gx);
+  const T* GY = static_cast<const T*>(d.Gy);
+  const T* PH = static_cast<const T*>(d.phi);
   const int2 lr = d.ecell[e];
   const T2 n = ld2(d.enrm, e);
   const T af = static_cast<const T*>(d.earea)[e];
   const T2 dl = ld2(d.edL, e);
   T pl[4], gxl[4], gyl[4], pfL[4], pfR[4];
-  ld4(P, lr.x, pl);
-  ld4(GX, lr.x, gxl);
-  ld4(GY, lr.x, gyl);
-  const T phiL = SPEC ? T(1) : PH[lr.x];
-  if (e < d.nint) {
+  ldc4<COH>(P, lr.x, pl);
+  ldc4<COH>(GX, lr.x, gxl);
+  ldc4<COH>(GY, lr.x, gyl);
+  const T phiL = SPEC ? T(1) : ldc1<COH>(PH, lr.x);
+  if (lr.y >= 0) {
     // src/residual.f90:83-92
     T pr[4], gxr[4], gyr[4];
-    ld4(P, lr.y, pr);
-    ld4(GX, lr.y, gxr);
-    ld4(GY, lr.y, gyr);
+    ldc4<COH>(P, lr.y, pr);
+    ldc4<COH>(GX, lr.y, gxr);
+    ldc4<COH>(GY, lr.y, gyr);
     const T2 dr = ld2(d.edR, e);
     if (SPEC) {
 #pragma unroll
@@ -417,7 +444,7 @@ __global__ void __launch_bounds__(256) k_flux(const DevView d, double dts) {
         pfR[v] = pr[v] + (dr.x * gxr[v] + dr.y * gyr[v]);
       }
     } else {
-      const T phiR = PH[lr.y];
+      const T phiR = ldc1<COH>(PH, lr.y);
       const T kh = TP(khalf), nkh = TP(nkhalf), omk = TP(omk);
 #pragma unroll
       for (int v = 0; v < 4; v++) {
@@ -432,9 +459,9 @@ __global__ void __launch_bounds__(256) k_flux(const DevView d, double dts) {
     // src/residual.f90:128-137
 #pragma unroll
     for (int v = 0; v < 4; v++) pfL[v] = pl[v] + phiL * (dl.x * gxl[v] + dl.y * gyl[v]);
-    const int bi = e - d.nint;
-    const T2 xy = ld2(d.exy, bi);
-    ghost_state(d, d.ebtype[bi], d.tctl[1] + dts, xy.x, xy.y, n.x, n.y, pfL, pfR);
+    // boundary record of the slot: type | case << 4, face centre
+    const T2 xy = ld2(d.exy, e);
+    ghost_state(d, d.ebtype[e], time, xy.x, xy.y, n.x, n.y, pfL, pfR);
   }
   T flux[4], wsm;
 #if FVS_STRICT
@@ -446,6 +473,12 @@ __global__ void __launch_bounds__(256) k_flux(const DevView d, double dts) {
   for (int v = 0; v < 4; v++) flux[v] = flux[v] * af;
   st4(static_cast<T*>(d.eflux), e, flux);
   static_cast<T*>(d.ews)[e] = wsm * af;
+}
+
+template <bool SPEC>
+__global__ void __launch_bounds__(256) k_flux(const DevView d, double dts) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e < d.nedge) flux_item<SPEC, false>(d, e, d.tctl[1] + dts);
 }
 
 // ---------------------------------------------------------------------------
@@ -462,7 +495,7 @@ __device__ __forceinline__ void two_sum(float& hi, float& lo, float x) {
   hi = s;
 }
 
-template <bool WS>
+template <bool WS, bool COH>
 __device__ __forceinline__ void cell_residual(const DevView& d, int ic, double* res, double& ws) {
   float hi[4] = {0.f, 0.f, 0.f, 0.f}, lo[4] = {0.f, 0.f, 0.f, 0.f}, wh = 0.f, wl = 0.f;
   const int4 cf = d.cflist[ic];
@@ -473,10 +506,10 @@ __device__ __forceinline__ void cell_residual(const DevView& d, int ic, double* 
     if (s == 0) continue;
     const int idx = (s > 0 ? s : -s) - 1;
     float f[4];
-    ld4(static_cast<const float*>(d.eflux), idx, f);
+    ldc4<COH>(static_cast<const float*>(d.eflux), idx, f);
 #pragma unroll
     for (int v = 0; v < 4; v++) two_sum(hi[v], lo[v], s > 0 ? f[v] : -f[v]);
-    if (WS) two_sum(wh, wl, static_cast<const float*>(d.ews)[idx]);
+    if (WS) two_sum(wh, wl, ldc1<COH>(static_cast<const float*>(d.ews), idx));
   }
   const double rv = -d.rvol[ic];
 #pragma unroll
@@ -484,12 +517,12 @@ __device__ __forceinline__ void cell_residual(const DevView& d, int ic, double* 
   ws = WS ? f2d_bits(wh) + f2d_bits(wl) : 0.0;
 }
 #else
-template <bool WS>
+template <bool WS, bool COH>
 __device__ __forceinline__ void gather_slot(const DevView& d, int s, double* r, double& ws) {
   if (s == 0) return;
   const int idx = (s > 0 ? s : -s) - 1;
   double f[4];
-  ld4(static_cast<const double*>(d.eflux), idx, f);
+  ldc4<COH>(static_cast<const double*>(d.eflux), idx, f);
   if (s > 0) {
 #pragma unroll
     for (int v = 0; v < 4; v++) r[v] = r[v] + f[v];
@@ -497,18 +530,18 @@ __device__ __forceinline__ void gather_slot(const DevView& d, int s, double* r, 
 #pragma unroll
     for (int v = 0; v < 4; v++) r[v] = r[v] - f[v];
   }
-  if (WS) ws = ws + static_cast<const double*>(d.ews)[idx];
+  if (WS) ws = ws + ldc1<COH>(static_cast<const double*>(d.ews), idx);
 }
 
-template <bool WS>
+template <bool WS, bool COH>
 __device__ __forceinline__ void cell_residual(const DevView& d, int ic, double* res, double& ws) {
   double r[4] = {0.0, 0.0, 0.0, 0.0};
   ws = 0.0;
   const int4 cf = d.cflist[ic];
-  gather_slot<WS>(d, cf.x, r, ws);
-  gather_slot<WS>(d, cf.y, r, ws);
-  gather_slot<WS>(d, cf.z, r, ws);
-  gather_slot<WS>(d, cf.w, r, ws);
+  gather_slot<WS, COH>(d, cf.x, r, ws);
+  gather_slot<WS, COH>(d, cf.y, r, ws);
+  gather_slot<WS, COH>(d, cf.z, r, ws);
+  gather_slot<WS, COH>(d, cf.w, r, ws);
 #if FVS_STRICT
   const double vol = d.vol[ic];
 #pragma unroll
@@ -564,14 +597,13 @@ __device__ __forceinline__ void block_sum4(const double* v, double* out) {
     for (int k = 0; k < 4; k++) out[k] = sh[k][0];
 }
 
-template <int MODE>
-__global__ void __launch_bounds__(256) k_update(const DevView d, const StageParams sp) {
-  const int ic = blockIdx.x * blockDim.x + threadIdx.x;
-  double d2[4] = {0.0, 0.0, 0.0, 0.0};
-  if (ic < d.nc) {
+// one cell of an RK stage; at the last stage adds |U-U0|^2 to d2
+template <int MODE, bool COH>
+__device__ __forceinline__ void update_item(const DevView& d, const StageParams& sp, int ic, double* d2) {
+  {
     double res[4], ws;
-    if (sp.steady && sp.stage == 1) cell_residual<true>(d, ic, res, ws);
-    else cell_residual<false>(d, ic, res, ws);
+    if (sp.steady && sp.stage == 1) cell_residual<true, COH>(d, ic, res, ws);
+    else cell_residual<false, COH>(d, ic, res, ws);
     double h = sp.h;
     if (sp.steady) {
       double dtl;
@@ -579,19 +611,19 @@ __global__ void __launch_bounds__(256) k_update(const DevView d, const StagePara
         dtl = d.cfl * d.vol[ic] / (0.5 * ws);
         d.dtl[ic] = dtl;
       } else {
-        dtl = d.dtl[ic];
+        dtl = ldc1<COH>(d.dtl, ic);
       }
       h = dtl * sp.cst;
     }
     double u0[4], u[4], f[4];
     if (sp.stage == 1) {
-      ld4(d.U, ic, u0);
+      ldc4<COH>(d.U, ic, u0);
       st4(d.U0, ic, u0);
 #pragma unroll
       for (int v = 0; v < 4; v++) f[v] = 0.0;
     } else {
-      ld4(d.U0, ic, u0);
-      if (MODE != MODE_SSP3) ld4(d.F, ic, f);
+      ldc4<COH>(d.U0, ic, u0);
+      if (MODE != MODE_SSP3) ldc4<COH>(d.F, ic, f);
     }
     if (MODE == MODE_SSP42) {
       // src/runge_kutta.f90:225-226 / :383-387
@@ -616,7 +648,7 @@ __global__ void __launch_bounds__(256) k_update(const DevView d, const StagePara
 #pragma unroll
         for (int v = 0; v < 4; v++) cur[v] = u0[v];
       } else {
-        ld4(d.U, ic, cur);
+        ldc4<COH>(d.U, ic, cur);
       }
 #pragma unroll
       for (int v = 0; v < 4; v++) {
@@ -632,10 +664,17 @@ __global__ void __launch_bounds__(256) k_update(const DevView d, const StagePara
 #pragma unroll
       for (int v = 0; v < 4; v++) {
         const double dd = fabs(u[v] - u0[v]);
-        d2[v] = dd * dd;
+        d2[v] += dd * dd;
       }
     }
   }
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(256) k_update(const DevView d, const StageParams sp) {
+  const int ic = blockIdx.x * blockDim.x + threadIdx.x;
+  double d2[4] = {0.0, 0.0, 0.0, 0.0};
+  if (ic < d.nc) update_item<MODE, false>(d, sp, ic, d2);
   if (sp.last) {
     double out[4];
     block_sum4(d2, out);
@@ -650,7 +689,7 @@ __global__ void __launch_bounds__(256) k_residual_out(const DevView d) {
   const int ic = blockIdx.x * blockDim.x + threadIdx.x;
   if (ic >= d.nc) return;
   double res[4], ws;
-  cell_residual<true>(d, ic, res, ws);
+  cell_residual<true, false>(d, ic, res, ws);
   st4(d.resid, ic, res);
   d.ws[ic] = ws;
 }
@@ -687,6 +726,135 @@ __global__ void __launch_bounds__(256) k_norm_final(const DevView d) {
     for (int k = 0; k < 4; k++) o[k] = sqrt(out[k] / double(d.nc));
     d.stepctl[0] = istep;
   }
+}
+
+// ---------------------------------------------------------------------------
+// persistent kernel: whole RK steps in one cooperative launch
+// ---------------------------------------------------------------------------
+// Bounded software grid barrier (all blocks are co-resident: cooperative
+// launch).  Returns false once any wait has run out of budget.
+__device__ __forceinline__ bool grid_sync(GridBarrier* gb, long long budget) {
+  __shared__ int s_ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    volatile unsigned int* vgen = &gb->gen;
+    volatile int* verr = &gb->err;
+    const unsigned int g = *vgen;
+    __threadfence();
+    const unsigned int arrived = atomicAdd(&gb->count, 1u) + 1u;
+    if (arrived == gridDim.x) {
+      atomicExch(&gb->count, 0u);
+      __threadfence();
+      atomicAdd(&gb->gen, 1u);
+    } else {
+      const long long t0 = clock64();
+      while (*vgen == g) {
+        if (*verr) break;
+        if (clock64() - t0 > budget) {
+          atomicExch(&gb->err, 1);
+          break;
+        }
+        __nanosleep(64);
+      }
+    }
+    __threadfence();
+    s_ok = (*verr == 0);
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
+
+template <int MODE>
+__device__ __forceinline__ void update_tile(const DevView& d, const PersistPlan& p, const StageParams& sp, int t) {
+  const int4 tl = p.cell_tiles[t];
+  double d2[4] = {0.0, 0.0, 0.0, 0.0};
+  for (int ic = tl.x + threadIdx.x; ic < tl.y; ic += blockDim.x) update_item<MODE, true>(d, sp, ic, d2);
+  if (sp.last) {
+    double out[4];
+    block_sum4(d2, out);
+    if (threadIdx.x == 0)
+#pragma unroll
+      for (int k = 0; k < 4; k++) p.tile_partials[4 * (size_t)t + k] = out[k];
+  }
+}
+
+template <int LIM, bool SPEC>
+__global__ void __launch_bounds__(256) k_persistent(const DevView d, const PersistPlan p) {
+  const int nb = gridDim.x;
+  const int step0 = *p.step0_dev;
+  for (int s = 0; s < p.nsteps; s++) {
+    const double told = p.t1 + double(step0 + s) * d.dt;
+    for (int k = 0; k < p.nstages; k++) {
+      const StageParams& sp = p.sp[k];
+      if (!d.first_order) {
+        for (int t = blockIdx.x; t < p.ncell_tiles; t += nb) {
+          const int4 tl = p.cell_tiles[t];
+          for (int ic = tl.x + threadIdx.x; ic < tl.y; ic += blockDim.x) gradient_item<FVS_GRAD_LSQ, LIM, true>(d, ic);
+        }
+        if (!grid_sync(p.bar, p.budget)) return;
+      }
+      for (int t = blockIdx.x; t < p.nedge_tiles; t += nb) {
+        const int2 tl = p.edge_tiles[t];
+        for (int e = tl.x + threadIdx.x; e < tl.y; e += blockDim.x) flux_item<SPEC, true>(d, e, told + sp.dts);
+      }
+      if (!grid_sync(p.bar, p.budget)) return;
+      for (int t = blockIdx.x; t < p.ncell_tiles; t += nb) {
+        if (sp.mode == MODE_SSP42) update_tile<MODE_SSP42>(d, p, sp, t);
+        else if (sp.mode == MODE_SSP3) update_tile<MODE_SSP3>(d, p, sp, t);
+        else update_tile<MODE_RK>(d, p, sp, t);
+      }
+      if (!grid_sync(p.bar, p.budget)) return;
+    }
+    // per-case RMS(dU) of this step from the tile partials (fixed order); the
+    // partials are rewritten only at the next step's last update phase
+    const int slot = (step0 + s) % p.norm_cap;
+    for (int c = blockIdx.x; c < p.ncase_active; c += nb) {
+      if (threadIdx.x == 0) {
+        const int4 ct = p.case_tiles[c];
+        double a[4] = {0.0, 0.0, 0.0, 0.0};
+        for (int t = ct.y; t < ct.z; t++)
+#pragma unroll
+          for (int k = 0; k < 4; k++) a[k] += p.tile_partials[4 * (size_t)t + k];
+        double* o = p.case_norms + 4 * ((size_t)ct.x * p.norm_cap + slot);
+#pragma unroll
+        for (int k = 0; k < 4; k++) o[k] = sqrt(a[k] / double(ct.w));
+      }
+    }
+  }
+}
+
+template <int LIM, bool SPEC>
+static cudaError_t launch_persistent_t(const DevView& d, const PersistPlan& p, int grid, int block, cudaStream_t s) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)grid);
+  cfg.blockDim = dim3((unsigned)block);
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, k_persistent<LIM, SPEC>, d, p);
+}
+
+static bool persistent_spec(const DevView& d) {
+  return !FVS_STRICT && d.khalf == 0.0 && d.omk == 1.0 && d.limiter == FVS_LIM_NONE && !d.first_order;
+}
+
+static int persistent_occupancy(const DevView& d, int block) {
+  if (d.grad_method != FVS_GRAD_LSQ) return 0;
+  int n = 0;
+  cudaError_t e;
+  if (d.limiter != FVS_LIM_NONE) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_persistent<1, false>, block, 0);
+  else if (persistent_spec(d)) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_persistent<0, true>, block, 0);
+  else e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_persistent<0, false>, block, 0);
+  return e == cudaSuccess ? n : 0;
+}
+
+static cudaError_t launch_persistent(const DevView& d, const PersistPlan& p, int grid, int block, cudaStream_t s) {
+  if (d.limiter != FVS_LIM_NONE) return launch_persistent_t<1, false>(d, p, grid, block, s);
+  if (persistent_spec(d)) return launch_persistent_t<0, true>(d, p, grid, block, s);
+  return launch_persistent_t<0, false>(d, p, grid, block, s);
 }
 
 // ---------------------------------------------------------------------------

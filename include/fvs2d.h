@@ -208,6 +208,38 @@ int fvs_launches_per_step(const fvs_handle* h, int32_t* n);
  * old->new (host copy, 0-based) for callers that keep data on the device. */
 int fvs_device_state(fvs_handle* h, void** dptr);
 
+/* ---- batched independent cases ------------------------------------------
+ * No counterpart in the reference, which runs one case per process: many
+ * cases (e.g. an airfoil sweep over Mach and angle of attack) advanced
+ * together.  All cases share the scheme flags of fvs_options (LSQ gradients,
+ * any precision, fixed dt or steady); only mach_inf / aoa_inf_deg differ.
+ * The meshes are preprocessed on host_threads threads (<= 0: all cores),
+ * packed as one disjoint union on the device, and advanced by one
+ * cooperative persistent kernel per chunk of steps (captured in a CUDA
+ * graph).  Every grid-barrier wait of that kernel is bounded; a wait that
+ * runs out returns FVS_ERR_TIMEOUT instead of hanging. */
+typedef struct fvs_batch fvs_batch;
+int fvs_batch_create(const fvs_mesh* meshes, const fvs_options* opts, int32_t ncases, int32_t host_threads,
+                     fvs_batch** out);
+void fvs_batch_destroy(fvs_batch* b);
+const char* fvs_batch_last_error(const fvs_batch* b);
+/* total cells and edge slots; launch4 = {block, tile, blocks per SM, graph} */
+int fvs_batch_info(const fvs_batch* b, int32_t* ncells, int32_t* nedges, int32_t* launch4);
+int fvs_batch_init_state(fvs_batch* b);                                  /* free stream per case */
+int fvs_batch_set_state(fvs_batch* b, int32_t icase, const double* cvar); /* [ncells_case][4] */
+int fvs_batch_get_state(fvs_batch* b, int32_t icase, double* cvar);
+/* times the launch-shape candidates on the batch (state restored after) */
+int fvs_batch_autotune(fvs_batch* b, int32_t trial_steps, float* best_ms_per_step);
+int fvs_batch_set_launch(fvs_batch* b, int32_t block, int32_t tile, int32_t blocks_per_sm);
+/* budget of one grid-barrier wait, seconds (default 4) */
+int fvs_batch_set_barrier_budget(fvs_batch* b, double seconds);
+/* nsteps (<= 1024) steps of every case; norms [ncases][nsteps][4] or NULL */
+int fvs_batch_steps(fvs_batch* b, int32_t nsteps, double* norms, float* ms);
+/* steps until each case's RMS(dU_rho) <= drop x its first value; converged
+ * cases leave the work lists.  steps_done [ncases]; first, last [ncases][4] */
+int fvs_batch_run_to_drop(fvs_batch* b, int32_t max_steps, double drop, int32_t chunk, int32_t* steps_done,
+                          double* first, double* last, float* ms);
+
 /* ---- allocation-free residual norm ---------------------------------------
  * No counterpart in the reference: an addition for callers that cannot
  * allocate device memory where they need the norm (hosts whose device memory
