@@ -97,3 +97,14 @@ class Batch:
         self._check(self._lib.fvs_batch_run_to_drop(self._h, int(max_steps), float(drop), int(chunk), capi.ptr(done),
                                                     capi.ptr(first), capi.ptr(last), C.byref(ms)))
         return done, first, last, ms.value
+
+    def run_to_level(self, max_steps: int, levels, chunk: int = 50):
+        """Steps until each case's RMS(dU_rho) <= levels[c]; same returns as run_to_drop."""
+        lv = np.ascontiguousarray(levels, np.float64)
+        done = np.zeros(self.ncases, np.int32)
+        first = np.zeros((self.ncases, 4))
+        last = np.zeros((self.ncases, 4))
+        ms = C.c_float(0)
+        self._check(self._lib.fvs_batch_run_to_level(self._h, int(max_steps), capi.ptr(lv), int(chunk), capi.ptr(done),
+                                                     capi.ptr(first), capi.ptr(last), C.byref(ms)))
+        return done, first, last, ms.value

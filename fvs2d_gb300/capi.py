@@ -98,6 +98,8 @@ SIGNATURES = {
     "fvs_batch_steps": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.POINTER(C.c_float)]),
     "fvs_batch_run_to_drop": (C.c_int, [C.c_void_p, C.c_int32, C.c_double, C.c_int32, C.c_void_p, C.c_void_p,
                                         C.c_void_p, C.POINTER(C.c_float)]),
+    "fvs_batch_run_to_level": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p,
+                                         C.c_void_p, C.POINTER(C.c_float)]),
     "fvs_rms_delta_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p]),
 }
 

@@ -538,8 +538,8 @@ int fvs_batch_autotune(fvs_batch* b, int32_t trial_steps, float* best_ms) {
 // Steps all cases until each one's RMS(dU_rho) falls to drop x its first
 // value (or max_steps).  steps_done[c] = the step at which case c reached the
 // drop (max_steps if it did not); first/last [ncases][4] norms.
-int fvs_batch_run_to_drop(fvs_batch* b, int32_t max_steps, double drop, int32_t chunk, int32_t* steps_done,
-                          double* first, double* last, float* ms) {
+static int run_until(fvs_batch* b, int32_t max_steps, double drop, const double* levels, int32_t chunk,
+                     int32_t* steps_done, double* first, double* last, float* ms) {
   if (!b || max_steps <= 0 || chunk <= 0 || chunk > b->norm_cap) return FVS_ERR_INVALID;
   const int nc = b->ncases;
   std::vector<double> f(4 * (size_t)nc, -1.0), l(4 * (size_t)nc, 0.0);
@@ -565,7 +565,7 @@ int fvs_batch_run_to_drop(fvs_batch* b, int32_t max_steps, double drop, int32_t 
         if (!std::isfinite(v[0])) { nonfinite = true; b->active[c] = 0; done[c] = step + s + 1; changed = true; break; }
         if (f[4 * c] < 0) std::memcpy(&f[4 * c], v, 32);
         std::memcpy(&l[4 * c], v, 32);
-        if (v[0] <= drop * f[4 * c]) {
+        if (v[0] <= (levels ? levels[c] : drop * f[4 * c])) {
           done[c] = step + s + 1;
           b->active[c] = 0;
           changed = true;
@@ -588,6 +588,17 @@ int fvs_batch_run_to_drop(fvs_batch* b, int32_t max_steps, double drop, int32_t 
   if (last) std::memcpy(last, l.data(), 32 * (size_t)nc);
   if (rc) return rc;
   return nonfinite ? b->fail(FVS_ERR_NONFINITE, "a case's residual norm is not finite") : FVS_OK;
+}
+
+int fvs_batch_run_to_drop(fvs_batch* b, int32_t max_steps, double drop, int32_t chunk, int32_t* steps_done,
+                          double* first, double* last, float* ms) {
+  return run_until(b, max_steps, drop, nullptr, chunk, steps_done, first, last, ms);
+}
+
+int fvs_batch_run_to_level(fvs_batch* b, int32_t max_steps, const double* levels, int32_t chunk, int32_t* steps_done,
+                           double* first, double* last, float* ms) {
+  if (!levels) return FVS_ERR_INVALID;
+  return run_until(b, max_steps, 0.0, levels, chunk, steps_done, first, last, ms);
 }
 
 }  // extern "C"

@@ -239,6 +239,10 @@ int fvs_batch_steps(fvs_batch* b, int32_t nsteps, double* norms, float* ms);
  * cases leave the work lists.  steps_done [ncases]; first, last [ncases][4] */
 int fvs_batch_run_to_drop(fvs_batch* b, int32_t max_steps, double drop, int32_t chunk, int32_t* steps_done,
                           double* first, double* last, float* ms);
+/* the same with an absolute target per case: RMS(dU_rho) <= levels[c]
+ * (a warm start judged on the threshold of a free-stream start) */
+int fvs_batch_run_to_level(fvs_batch* b, int32_t max_steps, const double* levels, int32_t chunk, int32_t* steps_done,
+                           double* first, double* last, float* ms);
 
 /* ---- allocation-free residual norm ---------------------------------------
  * No counterpart in the reference: an addition for callers that cannot
