@@ -30,6 +30,7 @@ UNITS = {
     "fvs_kern_mixed.cu": ["-fmad=true"],
     "fvs_noalloc.cu": [],
     "fvs_batch.cu": [],
+    "fvs_mlp.cu": [],
 }
 HEADERS = ["fvs_internal.hpp", "fvs_kernels.cuh", "fvs_layout.hpp"]
 

@@ -85,6 +85,10 @@ class Batch:
     def set_launch(self, block: int, tile: int, blocks_per_sm: int):
         self._check(self._lib.fvs_batch_set_launch(self._h, block, tile, blocks_per_sm))
 
+    def set_precision(self, precision: int):
+        """Switch all cases to another arithmetic (FP64 state kept)."""
+        self._check(self._lib.fvs_batch_set_precision(self._h, int(precision)))
+
     def set_barrier_budget(self, seconds: float):
         self._check(self._lib.fvs_batch_set_barrier_budget(self._h, float(seconds)))
 

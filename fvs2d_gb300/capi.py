@@ -94,12 +94,23 @@ SIGNATURES = {
     "fvs_batch_get_state": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p]),
     "fvs_batch_autotune": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_float)]),
     "fvs_batch_set_launch": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32]),
+    "fvs_batch_set_precision": (C.c_int, [C.c_void_p, C.c_int32]),
     "fvs_batch_set_barrier_budget": (C.c_int, [C.c_void_p, C.c_double]),
     "fvs_batch_steps": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.POINTER(C.c_float)]),
     "fvs_batch_run_to_drop": (C.c_int, [C.c_void_p, C.c_int32, C.c_double, C.c_int32, C.c_void_p, C.c_void_p,
                                         C.c_void_p, C.POINTER(C.c_float)]),
     "fvs_batch_run_to_level": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p,
                                          C.c_void_p, C.POINTER(C.c_float)]),
+    "fvs_mlp_create": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_uint64, C.POINTER(C.c_void_p)]),
+    "fvs_mlp_destroy": (None, [C.c_void_p]),
+    "fvs_mlp_last_error": (C.c_char_p, [C.c_void_p]),
+    "fvs_mlp_num_params": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64)]),
+    "fvs_mlp_get_params": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64]),
+    "fvs_mlp_set_params": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64]),
+    "fvs_mlp_loss_grad": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.POINTER(C.c_float), C.c_void_p]),
+    "fvs_mlp_train": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_int32, C.c_int32, C.c_float,
+                                C.c_uint64, C.c_void_p]),
+    "fvs_mlp_predict": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]),
     "fvs_rms_delta_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p]),
 }
 

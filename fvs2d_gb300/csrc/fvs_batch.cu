@@ -67,9 +67,16 @@ struct fvs_batch {
   std::string err;
   const KernelSet* ks = nullptr;
   bool mixed = false;
+  int prec = FVS_PREC_FP64;
   cudaStream_t stream = nullptr;
   DeviceArena arena;
-  DevView d;
+  DevView d;  // the current precision's view
+  // views of the other precisions, built on first use (the precision ladder)
+  struct Variant {
+    bool built = false;
+    DevView d;
+    int block = 256, tile = 1024, bps = 1;
+  } var[3];
   int nc = 0, ne = 0;
   std::vector<int> coff, eoff, cnum, enumv;  // per-case cell / edge-slot ranges
   std::vector<double> pinf;                 // [ncases][4]
@@ -119,33 +126,45 @@ struct fvs_batch {
 namespace {
 
 template <typename T>
-int build_batch_device(fvs_batch* B) {
+int build_batch_device(fvs_batch* B, DevView& d) {
   Layout<T> L;
   std::string err;
-  const bool fold_w = B->base.precision != FVS_PREC_FP64_STRICT;
+  const bool fold_w = d.grad_method == FVS_GRAD_LSQ && B->prec != FVS_PREC_FP64_STRICT;
+  const bool first = B->coff.empty();
   for (int c = 0; c < B->ncases; c++) {
     int rc = append_case(L, B->hm[c], fold_w, c, err);
     if (rc) return B->fail(rc, "case " + std::to_string(c) + ": " + err);
-    B->coff.push_back(L.case_coff[c]);
-    B->eoff.push_back(L.case_eoff[c]);
-    B->cnum.push_back(B->hm[c].nc);
-    B->enumv.push_back((int)(B->hm[c].edge_intr.size() + B->hm[c].b_edge.size()));
+    if (first) {
+      B->coff.push_back(L.case_coff[c]);
+      B->eoff.push_back(L.case_eoff[c]);
+      B->cnum.push_back(B->hm[c].nc);
+      B->enumv.push_back((int)(B->hm[c].edge_intr.size() + B->hm[c].b_edge.size()));
+    }
   }
   B->nc = L.nc;
   B->ne = L.ne;
   B->ref_off = B->coff;  // L.perm is appended case by case in the same order
-  DevView& d = B->d;
-  if (!upload_layout(B->arena, L, d) || !B->arena.upload(B->d_perm, L.perm))
-    return B->fail(FVS_ERR_NOMEM, "device allocation or upload of the batch meshes failed");
+  if (!upload_layout(B->arena, L, d)) return B->fail(FVS_ERR_NOMEM, "device allocation or upload of the batch meshes failed");
+  if (first && !B->arena.upload(B->d_perm, L.perm)) return B->fail(FVS_ERR_NOMEM, "upload of the cell maps failed");
   double* dp = nullptr;
   if (!B->arena.upload(dp, B->pinf)) return B->fail(FVS_ERR_NOMEM, "upload of the free streams failed");
   d.case_pinf = dp;
+  if (!alloc_work<T>(B->arena, d, L.nc, L.ne, (L.nc + 255) / 256, 16))
+    return B->fail(FVS_ERR_NOMEM, "device allocation of the batch state failed");
+  std::vector<T> phi0(L.nc, T(d.first_order ? 0.0 : 1.0));
+  if (cudaMemcpy(d.phi, phi0.data(), sizeof(T) * L.nc, cudaMemcpyHostToDevice) != cudaSuccess)
+    return B->fail(FVS_ERR_CUDA, "phi upload failed");
+  std::vector<double> dtl(L.nc, B->base.dt);
+  if (cudaMemcpy(d.dtl, dtl.data(), 8 * dtl.size(), cudaMemcpyHostToDevice) != cudaSuccess)
+    return B->fail(FVS_ERR_CUDA, "dt upload failed");
+  return FVS_OK;
+}
+
+int alloc_batch_buffers(fvs_batch* B) {
   void* p;
-  const int nblk = (L.nc + 255) / 256;
-  bool ok = alloc_work<T>(B->arena, d, L.nc, L.ne, nblk, 16);
-  ok = ok && B->arena.alloc(p, 32 * (size_t)L.nc);
+  bool ok = B->arena.alloc(p, 32 * (size_t)B->nc);
   B->d_stage = static_cast<double*>(p);
-  ok = ok && B->arena.alloc(p, 32 * (size_t)L.nc);
+  ok = ok && B->arena.alloc(p, 32 * (size_t)B->nc);
   B->d_backup = static_cast<double*>(p);
   ok = ok && B->arena.alloc(p, 32 * (size_t)B->ncases * B->norm_cap);
   B->d_case_norms = static_cast<double*>(p);
@@ -155,14 +174,25 @@ int build_batch_device(fvs_batch* B) {
   B->d_step0 = static_cast<int*>(p);
   ok = ok && B->arena.alloc(p, 16 * (size_t)B->ncases);
   B->d_case_tiles = static_cast<int4*>(p);
-  if (!ok) return B->fail(FVS_ERR_NOMEM, "device allocation of the batch state failed");
-  std::vector<T> phi0(L.nc, T(B->base.reconst == FVS_RECON_UPWIND1 ? 0.0 : 1.0));
-  if (cudaMemcpy(d.phi, phi0.data(), sizeof(T) * L.nc, cudaMemcpyHostToDevice) != cudaSuccess)
-    return B->fail(FVS_ERR_CUDA, "phi upload failed");
-  std::vector<double> dtl(L.nc, B->base.dt);
-  if (cudaMemcpy(d.dtl, dtl.data(), 8 * dtl.size(), cudaMemcpyHostToDevice) != cudaSuccess)
-    return B->fail(FVS_ERR_CUDA, "dt upload failed");
-  return FVS_OK;
+  return ok ? FVS_OK : B->fail(FVS_ERR_NOMEM, "device allocation of the batch buffers failed");
+}
+
+void init_view_constants(fvs_batch* B, DevView& d) {
+  const fvs_options& ob = B->base;
+  d.gamma = ob.gamma; d.gm1 = ob.gamma - 1.0; d.igm1 = 1.0 / (ob.gamma - 1.0);
+  d.khalf = ob.umuscl / 2.0; d.nkhalf = -ob.umuscl / 2.0; d.omk = 1.0 - ob.umuscl; d.cfl = ob.cfl;
+  d.fgamma = float(d.gamma); d.fgm1 = float(d.gm1); d.figm1 = float(d.igm1);
+  d.fkhalf = float(d.khalf); d.fnkhalf = float(d.nkhalf); d.fomk = float(d.omk);
+  d.limiter = ob.limiter; d.grad_method = ob.grad_method; d.first_order = ob.reconst == FVS_RECON_UPWIND1;
+  d.vortex = ob.vortex; d.vx = ob.vortex_x; d.vy = ob.vortex_y; d.vkappa = ob.vortex_kappa;
+  for (int k = 0; k < 4; k++) { d.vinf[k] = ob.vortex_inf[k]; d.pinf[k] = B->pinf[k]; }
+  mms_constants(d.mc);
+  d.dt = ob.dt;
+}
+
+const KernelSet* kernels_for(int prec) {
+  return prec == FVS_PREC_MIXED ? &kernels_mixed()
+         : (prec == FVS_PREC_FP64_STRICT ? &kernels_fp64_strict() : &kernels_fp64_fast());
 }
 
 void set_batch_stages(fvs_batch* B) {
@@ -367,26 +397,18 @@ int fvs_batch_create(const fvs_mesh* meshes, const fvs_options* opts, int32_t nc
     B->pinf[4 * c + 2] = opts[c].mach_inf * std::sin(aoa);
     B->pinf[4 * c + 3] = 1.0 / opts[c].gamma;
   }
+  B->prec = o0.precision;
   B->mixed = o0.precision == FVS_PREC_MIXED;
-  B->ks = B->mixed ? &kernels_mixed()
-          : (o0.precision == FVS_PREC_FP64_STRICT ? &kernels_fp64_strict() : &kernels_fp64_fast());
+  B->ks = kernels_for(o0.precision);
   cudaError_t e = cudaStreamCreateWithFlags(&B->stream, cudaStreamNonBlocking);
   if (e != cudaSuccess) { g_batch_create_error = std::string("cudaStreamCreate: ") + cudaGetErrorString(e); return FVS_ERR_CUDA; }
   cudaMallocHost(&B->h_step0, 16);
   cudaEventCreate(&B->ev0);
   cudaEventCreate(&B->ev1);
   cudaDeviceGetAttribute(&B->nsm, cudaDevAttrMultiProcessorCount, 0);
-  DevView& d = B->d;
-  const fvs_options& ob = B->base;
-  d.gamma = ob.gamma; d.gm1 = ob.gamma - 1.0; d.igm1 = 1.0 / (ob.gamma - 1.0);
-  d.khalf = ob.umuscl / 2.0; d.nkhalf = -ob.umuscl / 2.0; d.omk = 1.0 - ob.umuscl; d.cfl = ob.cfl;
-  d.fgamma = float(d.gamma); d.fgm1 = float(d.gm1); d.figm1 = float(d.igm1);
-  d.fkhalf = float(d.khalf); d.fnkhalf = float(d.nkhalf); d.fomk = float(d.omk);
-  d.limiter = ob.limiter; d.grad_method = ob.grad_method; d.first_order = ob.reconst == FVS_RECON_UPWIND1;
-  d.vortex = ob.vortex; d.vx = ob.vortex_x; d.vy = ob.vortex_y; d.vkappa = ob.vortex_kappa;
-  for (int k = 0; k < 4; k++) { d.vinf[k] = ob.vortex_inf[k]; d.pinf[k] = B->pinf[k]; }
-  mms_constants(d.mc);
-  int rc = B->mixed ? build_batch_device<float>(B.get()) : build_batch_device<double>(B.get());
+  init_view_constants(B.get(), B->d);
+  int rc = B->mixed ? build_batch_device<float>(B.get(), B->d) : build_batch_device<double>(B.get(), B->d);
+  if (!rc) rc = alloc_batch_buffers(B.get());
   if (rc) { g_batch_create_error = B->err; return rc; }
   set_batch_stages(B.get());
   B->active.assign(ncases, 1);
@@ -453,6 +475,43 @@ int fvs_batch_init_state(fvs_batch* b) {
     if (rc) return rc;
   }
   return FVS_OK;
+}
+
+// Switches the batch to another arithmetic (the precision ladder: a mixed
+// phase followed by an FP64 phase).  The other precision's device layout is
+// built on first use from the stored host meshes; the FP64 state is copied.
+int fvs_batch_set_precision(fvs_batch* b, int32_t precision) {
+  if (!b || precision < 0 || precision > 2) return FVS_ERR_INVALID;
+  if (precision == b->prec) return FVS_OK;
+  fvs_batch::Variant& cur = b->var[b->prec];
+  cur.built = true;
+  cur.d = b->d;
+  cur.block = b->block; cur.tile = b->tile; cur.bps = b->bps;
+  fvs_batch::Variant& nxt = b->var[precision];
+  const int old_prec = b->prec;
+  b->prec = precision;
+  if (!nxt.built) {
+    init_view_constants(b, nxt.d);
+    int rc = precision == FVS_PREC_MIXED ? build_batch_device<float>(b, nxt.d) : build_batch_device<double>(b, nxt.d);
+    if (rc) {
+      b->prec = old_prec;
+      return rc;
+    }
+    nxt.built = true;
+    nxt.block = b->block; nxt.tile = b->tile; nxt.bps = b->bps;
+  }
+  cudaError_t e = cudaMemcpyAsync(nxt.d.U, cur.d.U, 32 * (size_t)b->nc, cudaMemcpyDeviceToDevice, b->stream);
+  if (e != cudaSuccess) return b->cuda_fail(e, "state copy");
+  b->d = nxt.d;
+  b->ks = kernels_for(precision);
+  b->mixed = precision == FVS_PREC_MIXED;
+  b->block = nxt.block; b->tile = nxt.tile; b->bps = nxt.bps;
+  b->ks->cvar2pvar(b->d, b->stream);
+  if (b->graph) { cudaGraphExecDestroy(b->graph); b->graph = nullptr; }
+  b->graph_steps = -1;
+  b->plan_dirty = true;
+  e = cudaStreamSynchronize(b->stream);
+  return e == cudaSuccess ? FVS_OK : b->cuda_fail(e, "precision switch");
 }
 
 int fvs_batch_set_barrier_budget(fvs_batch* b, double seconds) {

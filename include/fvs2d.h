@@ -231,6 +231,9 @@ int fvs_batch_get_state(fvs_batch* b, int32_t icase, double* cvar);
 /* times the launch-shape candidates on the batch (state restored after) */
 int fvs_batch_autotune(fvs_batch* b, int32_t trial_steps, float* best_ms_per_step);
 int fvs_batch_set_launch(fvs_batch* b, int32_t block, int32_t tile, int32_t blocks_per_sm);
+/* switches the arithmetic of all cases (FVS_PREC_*), keeping the FP64
+ * state: e.g. MIXED until the FP32 flux floor, then FP64 to a 1e-10 drop */
+int fvs_batch_set_precision(fvs_batch* b, int32_t precision);
 /* budget of one grid-barrier wait, seconds (default 4) */
 int fvs_batch_set_barrier_budget(fvs_batch* b, double seconds);
 /* nsteps (<= 1024) steps of every case; norms [ncases][nsteps][4] or NULL */
@@ -243,6 +246,24 @@ int fvs_batch_run_to_drop(fvs_batch* b, int32_t max_steps, double drop, int32_t 
  * (a warm start judged on the threshold of a free-stream start) */
 int fvs_batch_run_to_level(fvs_batch* b, int32_t max_steps, const double* levels, int32_t chunk, int32_t* steps_done,
                            double* first, double* last, float* ms);
+
+/* ---- learned warm start: a small MLP on the GPU ---------------------------
+ * No counterpart in the reference.  n_in -> width (GELU) x depth -> n_out,
+ * FP32 master weights, BF16 tensor-core GEMMs with FP32 accumulation, Adam
+ * on the mean squared error, all on the GPU.  Parameters in the unpadded
+ * layout: for each layer W[out][in] then b[out]. */
+typedef struct fvs_mlp fvs_mlp;
+int fvs_mlp_create(int32_t n_in, int32_t width, int32_t depth, int32_t n_out, uint64_t seed, fvs_mlp** out);
+void fvs_mlp_destroy(fvs_mlp* m);
+const char* fvs_mlp_last_error(const fvs_mlp* m);
+int fvs_mlp_num_params(const fvs_mlp* m, int64_t* n);
+int fvs_mlp_get_params(fvs_mlp* m, float* dst, int64_t n);
+int fvs_mlp_set_params(fvs_mlp* m, const float* src, int64_t n);
+/* loss and gradients of one batch x[n][n_in], y[n][n_out], no update */
+int fvs_mlp_loss_grad(fvs_mlp* m, const float* x, const float* y, int32_t n, float* loss, float* grads);
+int fvs_mlp_train(fvs_mlp* m, const float* x, const float* y, int64_t n, int32_t batch, int32_t epochs, float lr,
+                  uint64_t seed, float* loss_per_epoch);
+int fvs_mlp_predict(fvs_mlp* m, const float* x, int64_t n, float* y);
 
 /* ---- allocation-free residual norm ---------------------------------------
  * No counterpart in the reference: an addition for callers that cannot

@@ -1,0 +1,60 @@
+"""The warm-start MLP on the GPU: gradients against the CPU oracle
+(oracle/mlp_oracle.py, float64 replaying the BF16 roundings) and training
+that actually fits a smooth target."""
+import os
+import sys
+
+import numpy as np
+import pytest
+
+from fvs2d_gb300.mlp import MLP
+
+sys.path.insert(0, os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "oracle"))
+import mlp_oracle  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("n,n_in,width,depth,n_out", [(64, 5, 32, 2, 4), (300, 5, 256, 4, 4), (257, 7, 48, 1, 3)])
+def test_gradients_match_cpu_oracle(n, n_in, width, depth, n_out):
+    rng = np.random.default_rng(11)
+    m = MLP(n_in, width, depth, n_out, seed=3)
+    x = rng.standard_normal((n, n_in)).astype(np.float32)
+    y = rng.standard_normal((n, n_out)).astype(np.float32) * 0.3
+    p = m.get_params()
+    loss, g = m.loss_grad(x, y)
+    ref_loss, ref_g = mlp_oracle.loss_grad(p, x.astype(np.float64), y.astype(np.float64), n_in, width, depth, n_out)
+    assert abs(loss - ref_loss) <= 1e-3 * abs(ref_loss)
+    err = np.linalg.norm(g - ref_g) / np.linalg.norm(ref_g)
+    assert err < 1e-2, err
+    # every layer's gradient, not only the largest
+    off = 0
+    dims_in = [n_in] + [width] * depth
+    dims_out = [width] * depth + [n_out]
+    for i, o in zip(dims_in, dims_out):
+        k = i * o + o
+        e = np.linalg.norm(g[off:off + k] - ref_g[off:off + k]) / max(np.linalg.norm(ref_g[off:off + k]), 1e-30)
+        assert e < 3e-2, (i, o, e)
+        off += k
+
+
+def test_params_roundtrip():
+    m = MLP(5, 64, 2, 4, seed=1)
+    p = m.get_params()
+    q = p * 0.5 + 0.01
+    m.set_params(q)
+    assert np.array_equal(m.get_params(), q.astype(np.float32))
+
+
+def test_training_fits_smooth_target():
+    rng = np.random.default_rng(5)
+    x = rng.uniform(-1, 1, (65536, 5)).astype(np.float32)
+    y = np.stack([np.sin(2 * x[:, 0]) * x[:, 1], x[:, 2] ** 2 - x[:, 3], np.cos(x[:, 4] + x[:, 0]),
+                  0.5 * x[:, 1] * x[:, 2]], 1).astype(np.float32)
+    m = MLP(5, 256, 4, 4, seed=2)
+    base = float(((m.predict(x[:4096]) - y[:4096]) ** 2).mean())
+    losses = m.train(x, y, batch=2048, epochs=12, lr=2e-3, seed=1)
+    assert np.all(np.isfinite(losses))
+    pred = m.predict(x[:4096])
+    mse = float(((pred - y[:4096]) ** 2).mean())
+    assert mse < 0.02 * base and mse < 2e-3, (base, mse, losses)
