@@ -334,7 +334,17 @@ def main():
     ap.add_argument("--no-variants", dest="variants", action="store_false")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=12.0)
+    ap.add_argument("--workload", default="vortex", choices=["vortex", "sweep"],
+                    help="vortex: the 1,048,576-cell throughput case (default); sweep: time to a 1e-10 drop on an "
+                         "airfoil sweep, plain FP64 vs batched ladder vs learned warm start")
+    ap.add_argument("--n-train", type=int, default=96)
+    ap.add_argument("--n-test", type=int, default=24)
     args = ap.parse_args()
+    if args.workload == "sweep":
+        from fvs2d_gb300 import _build, sweep_bench
+        _build.build()
+        print(json.dumps(sweep_bench.run(args.n_train, args.n_test)), flush=True)
+        return
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3
     out = run_reference(args) if args.impl == "reference" else run_ours(args)

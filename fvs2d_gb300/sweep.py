@@ -77,9 +77,10 @@ def free_stream_state(c: Case, ncells: int, gamma: float = 1.4) -> np.ndarray:
     return np.tile(np.array([rho, rho * u, rho * v, e]), (ncells, 1))
 
 
-def run_plain(cases, precision, max_steps, drop, starts=None, ref_levels=None, check_every=200):
+def run_plain(cases, precision, max_steps, drop, starts=None, ref_levels=None, check_every=200, states=None):
     """One Solver per case, one after the other (the plain path).  Returns
-    per-case steps, wall seconds total, and the first-step residuals."""
+    per-case steps, wall seconds total, and the first-step residuals; the
+    final states are appended to `states` when a list is given."""
     from .solver import Solver
     steps, firsts = [], []
     t0 = time.perf_counter()
@@ -91,6 +92,8 @@ def run_plain(cases, precision, max_steps, drop, starts=None, ref_levels=None, c
             n, log = _run_absolute(s, max_steps, drop, ref_levels[k] if ref_levels is not None else None, check_every)
             steps.append(n)
             firsts.append(log[0, 0])
+            if states is not None:
+                states.append(s.cvar)
     return np.array(steps), time.perf_counter() - t0, np.array(firsts)
 
 

@@ -1,0 +1,95 @@
+"""Time-to-residual-drop on an airfoil sweep: plain FP64 vs batched +
+mixed/FP64 ladder + learned warm start (the second half of the headline
+metric).  Runs entirely on the GPU through the C-ABI; prints one JSON object.
+
+  train   n_train cases (seed 5) solved by the batched ladder; their
+          converged cells train the warm-start MLP on the GPU
+  test    n_test held-out cases (seed 6), each solved three ways to the same
+          absolute target, 1e-10 x the first-step RMS(dU_rho) of a
+          free-stream start:
+            plain    one FP64 Solver per case, one after the other
+            batched  one batch, mixed until 1e-5 x target level, then FP64
+            learned  the same batch started from the network's prediction
+          errors: max |U - U_plain| / max|U_plain| of the final states, and
+          the surrogate's error before any solver step
+"""
+from __future__ import annotations
+
+import json
+import time
+
+import numpy as np
+
+from . import PREC_FP64, PREC_MIXED, sweep
+from .warmstart import WarmStart, build_dataset, reference_levels, solve_ladder
+
+
+def run(n_train=96, n_test=24, wall=(64, 192), radial=(32, 96), max_steps=200000, epochs=30, seed_train=5,
+        seed_test=6, drop=1e-10, switch=1e-5):
+    out = {"distribution": {"wall": wall, "radial": radial, "mach": [0.3, 0.85], "aoa_deg": [-2, 4],
+                            "n_train": n_train, "n_test": n_test, "seeds": [seed_train, seed_test]},
+           "scheme": "steady SSP-RK(4,2), local dt CFL 1.25, first-order Roe (the reference's second-order "
+                     "limited scheme stalls on these meshes), slip wall + free stream"}
+    # ---- training data: converged solutions of the training sweep
+    train = sweep.draw_cases(n_train, seed_train, wall, radial)
+    tm = [c.mesh() for c in train]
+    t0 = time.perf_counter()
+    lv = reference_levels(train, tm)
+    states, n1, n2, t_solve, _ = solve_ladder(tm, [sweep.case_options(c, PREC_MIXED) for c in train], lv, switch, drop,
+                                              max_steps)
+    X, Y = build_dataset(train, states)
+    t1 = time.perf_counter()
+    ws = WarmStart(width=256, depth=4, seed=1)
+    losses = ws.fit(X, Y, epochs=epochs, batch=4096, lr=1e-3, seed=2)
+    t_train = time.perf_counter() - t1
+    out["training"] = {"cells_train": int(sum(m.ncells for m in tm)), "samples": int(X.shape[0]),
+                       "solve_seconds": round(t_solve, 2), "train_seconds": round(t_train, 2),
+                       "loss_first_last": [float(losses[0]), float(losses[-1])],
+                       "data_seconds": round(t1 - t0, 2)}
+    # ---- held-out sweep
+    test = sweep.draw_cases(n_test, seed_test, wall, radial)
+    meshes = [c.mesh() for c in test]
+    levels = reference_levels(test, meshes)
+    plain_states = []
+    steps_p, t_plain, firsts = sweep.run_plain(test, PREC_FP64, max_steps, drop, ref_levels=levels, check_every=500,
+                                               states=plain_states)
+    st_b, b1, b2, t_batch, _ = solve_ladder(meshes, [sweep.case_options(c, PREC_MIXED) for c in test], levels, switch, drop,
+                                            max_steps)
+    starts = [ws.predict_state(c, m) for c, m in zip(test, meshes)]
+    st_l, l1, l2, t_learn, _ = solve_ladder(meshes, [sweep.case_options(c, PREC_MIXED) for c in test], levels, switch,
+                                            drop, max_steps, starts=starts)
+
+    def err(a, b):
+        return float(max(np.abs(x - y).max() / np.abs(y).max() for x, y in zip(a, b)))
+
+    sur_inf = float(max(np.abs(s - p).max() / np.abs(p).max() for s, p in zip(starts, plain_states)))
+    sur_l2 = float(np.sqrt(np.mean([((s - p) ** 2).mean() / (p ** 2).mean() for s, p in zip(starts, plain_states)])))
+    fs = [sweep.free_stream_state(c, m.ncells) for c, m in zip(test, meshes)]
+    fs_inf = float(max(np.abs(s - p).max() / np.abs(p).max() for s, p in zip(fs, plain_states)))
+    out["test"] = {
+        "cells_test": int(sum(m.ncells for m in meshes)),
+        "plain_fp64": {"seconds": round(t_plain, 3), "steps_total": int(steps_p.sum())},
+        "batched_ladder": {"seconds": round(t_batch, 3), "steps_mixed": int(b1.max()), "steps_fp64": int(b2.max()),
+                           "linf_vs_plain": err(st_b, plain_states)},
+        "learned_batched_ladder": {"seconds": round(t_learn, 3), "steps_mixed": int(l1.max()), "steps_fp64": int(l2.max()),
+                                   "linf_vs_plain": err(st_l, plain_states)},
+        "speedup_batched_vs_plain": round(t_plain / t_batch, 2),
+        "speedup_learned_vs_plain": round(t_plain / t_learn, 2),
+        "surrogate_error": {"linf_rel": sur_inf, "l2_rel": sur_l2, "free_stream_linf_rel": fs_inf},
+        "steps_per_case_plain": steps_p.tolist(),
+    }
+    return out
+
+
+def main(argv=None):
+    import argparse
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--n-train", type=int, default=96)
+    ap.add_argument("--n-test", type=int, default=24)
+    ap.add_argument("--epochs", type=int, default=30)
+    a = ap.parse_args(argv)
+    print(json.dumps(run(a.n_train, a.n_test, epochs=a.epochs)), flush=True)
+
+
+if __name__ == "__main__":
+    main()

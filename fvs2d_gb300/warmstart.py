@@ -1,0 +1,113 @@
+"""Learned warm start for airfoil sweeps.
+
+A network maps per-cell features (Mach, angle of attack, the cell centroid
+x, y and the wall distance) to the converged conservative state; the solver
+starts from its prediction instead of the free stream and still iterates to
+the same absolute residual threshold, so the network only changes how many
+steps are needed, never the answer.  Training data are converged solutions
+the solver itself produces; training and inference run on the GPU
+(fvs2d_gb300.mlp).
+
+The fast solve is the precision ladder on a batch: mixed precision until
+each case's RMS(dU_rho) reaches `switch` x its reference level (the FP32 flux
+floor lies near 5e-6 of it), then FP64 to `drop` x the reference level.
+"""
+from __future__ import annotations
+
+import time
+
+import numpy as np
+
+from . import PREC_FP64, PREC_MIXED, sweep
+from .batch import Batch
+from .mlp import MLP
+
+N_FEATURES = 5
+
+
+def cell_centroids(mesh) -> np.ndarray:
+    t = mesh.tri_nodes - 1
+    return mesh.node_xy[t].mean(1)
+
+
+def features(case: sweep.Case, mesh) -> np.ndarray:
+    xy = cell_centroids(mesh)
+    d = sweep.wall_distance(mesh, case.nw, xy)
+    r = np.hypot(xy[:, 0] - 0.5, xy[:, 1])
+    f = np.empty((xy.shape[0], N_FEATURES), np.float32)
+    f[:, 0] = (case.mach - 0.575) / 0.16
+    f[:, 1] = (case.aoa - 1.0) / 1.75
+    f[:, 2] = (xy[:, 0] - 0.5) / (0.5 + r)
+    f[:, 3] = xy[:, 1] / (0.5 + r)
+    f[:, 4] = np.log10(d + 1e-4) / 2.0
+    return f
+
+
+def targets(case: sweep.Case, cvar: np.ndarray) -> np.ndarray:
+    return (cvar - sweep.free_stream_state(case, cvar.shape[0])).astype(np.float32)
+
+
+def solve_ladder(meshes, opts_mixed, levels, switch=1e-5, drop=1e-10, max_steps=200000, chunk=200, starts=None,
+                 autotune=True):
+    """Batched precision-ladder solve to levels*drop (levels: per-case
+    reference residuals).  Returns (states, steps_mixed, steps_fp64, seconds)."""
+    t0 = time.perf_counter()
+    with Batch(meshes, opts_mixed) as b:
+        b.initialize_solution()
+        if starts is not None:
+            for c, u in enumerate(starts):
+                b.set_state(c, u)
+        if autotune:
+            b.autotune(2)
+            if starts is not None:
+                for c, u in enumerate(starts):
+                    b.set_state(c, u)
+        n1, _, _, _ = b.run_to_level(max_steps, np.asarray(levels) * switch, chunk)
+        b.set_precision(PREC_FP64)
+        n2, _, last, _ = b.run_to_level(max_steps, np.asarray(levels) * drop, chunk)
+        states = [b.get_state(c) for c in range(b.ncases)]
+    return states, n1, n2, time.perf_counter() - t0, last
+
+
+def reference_levels(cases, meshes):
+    """First-step RMS(dU_rho) of a free-stream start (the plain path's first
+    residual), one short FP64 batch step."""
+    with Batch(meshes, [sweep.case_options(c, PREC_FP64) for c in cases]) as b:
+        b.initialize_solution()
+        norms, _ = b.steps(1)
+    return norms[:, 0, 0].copy()
+
+
+class WarmStart:
+    def __init__(self, width=256, depth=4, seed=0):
+        self.net = MLP(N_FEATURES, width, depth, 4, seed=seed)
+        self.scale = np.ones(4, np.float32)
+
+    def fit(self, X, Y, epochs=20, batch=4096, lr=1e-3, seed=0):
+        self.scale = np.maximum(Y.std(0), 1e-6).astype(np.float32)
+        return self.net.train(X, Y / self.scale, batch=batch, epochs=epochs, lr=lr, seed=seed)
+
+    def predict_state(self, case: sweep.Case, mesh) -> np.ndarray:
+        f = features(case, mesh)
+        dU = self.net.predict(f) * self.scale
+        u = sweep.free_stream_state(case, f.shape[0]) + dU.astype(np.float64)
+        # keep the state physical (positive density and pressure)
+        u[:, 0] = np.maximum(u[:, 0], 0.05)
+        ke = 0.5 * (u[:, 1] ** 2 + u[:, 2] ** 2) / u[:, 0]
+        u[:, 3] = np.maximum(u[:, 3], ke + 0.05 / 0.4)
+        return u
+
+
+def build_dataset(cases, states, max_cells_per_case=20000, seed=0):
+    rng = np.random.default_rng(seed)
+    X, Y = [], []
+    for c, u in zip(cases, states):
+        mesh = c.mesh()
+        f = features(c, mesh)
+        t = targets(c, u)
+        if f.shape[0] > max_cells_per_case:
+            sel = rng.choice(f.shape[0], max_cells_per_case, replace=False)
+            f, t = f[sel], t[sel]
+        X.append(f)
+        Y.append(t)
+    return np.concatenate(X), np.concatenate(Y)
