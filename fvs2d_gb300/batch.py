@@ -103,8 +103,9 @@ class Batch:
         return done, first, last, ms.value
 
     def run_to_level(self, max_steps: int, levels, chunk: int = 50):
-        """Steps until each case's RMS(dU_rho) <= levels[c]; same returns as run_to_drop."""
-        lv = np.ascontiguousarray(levels, np.float64)
+        """Steps until each case's RMS(dU_k) <= levels[c, k] for all k; same returns as run_to_drop."""
+        lv = np.ascontiguousarray(np.broadcast_to(np.asarray(levels, np.float64).reshape(self.ncases, -1),
+                                                  (self.ncases, 4)), np.float64)
         done = np.zeros(self.ncases, np.int32)
         first = np.zeros((self.ncases, 4))
         last = np.zeros((self.ncases, 4))

@@ -624,7 +624,11 @@ static int run_until(fvs_batch* b, int32_t max_steps, double drop, const double*
         if (!std::isfinite(v[0])) { nonfinite = true; b->active[c] = 0; done[c] = step + s + 1; changed = true; break; }
         if (f[4 * c] < 0) std::memcpy(&f[4 * c], v, 32);
         std::memcpy(&l[4 * c], v, 32);
-        if (v[0] <= (levels ? levels[c] : drop * f[4 * c])) {
+        // converged when every component is at its target (one component can
+        // dip under its level while an oscillating mode passes through zero)
+        bool conv = true;
+        for (int k = 0; k < 4; k++) conv = conv && v[k] <= (levels ? levels[4 * c + k] : drop * f[4 * c + k]);
+        if (conv) {
           done[c] = step + s + 1;
           b->active[c] = 0;
           changed = true;

@@ -91,22 +91,24 @@ def run_plain(cases, precision, max_steps, drop, starts=None, ref_levels=None, c
                 s.cvar = starts[k]
             n, log = _run_absolute(s, max_steps, drop, ref_levels[k] if ref_levels is not None else None, check_every)
             steps.append(n)
-            firsts.append(log[0, 0])
+            firsts.append(log[0])
             if states is not None:
                 states.append(s.cvar)
     return np.array(steps), time.perf_counter() - t0, np.array(firsts)
 
 
 def _run_absolute(s, max_steps, drop, ref_level, check_every):
+    """Steps until RMS(dU_k) <= drop * ref_level[k] in all four components
+    (ref_level None: the first step's norms)."""
     logs, done = [], 0
-    first = ref_level
+    first = None if ref_level is None else np.broadcast_to(np.asarray(ref_level, np.float64), (4,))
     while done < max_steps:
         n = min(check_every, max_steps - done)
         log = s.time_integration(0.0, n)
         logs.append(log)
         if first is None:
-            first = log[0, 0]
-        hit = np.nonzero(log[:, 0] <= drop * first)[0]
+            first = log[0].copy()
+        hit = np.nonzero(np.all(log <= drop * first[None, :], axis=1))[0]
         if hit.size:
             done += int(hit[0]) + 1
             logs[-1] = log[: int(hit[0]) + 1]

@@ -62,6 +62,9 @@ def run(n_train=96, n_test=24, wall=(64, 192), radial=(32, 96), max_steps=200000
     def err(a, b):
         return float(max(np.abs(x - y).max() / np.abs(y).max() for x, y in zip(a, b)))
 
+    def per_case(a, b):
+        return [float(np.abs(x - y).max() / np.abs(y).max()) for x, y in zip(a, b)]
+
     sur_inf = float(max(np.abs(s - p).max() / np.abs(p).max() for s, p in zip(starts, plain_states)))
     sur_l2 = float(np.sqrt(np.mean([((s - p) ** 2).mean() / (p ** 2).mean() for s, p in zip(starts, plain_states)])))
     fs = [sweep.free_stream_state(c, m.ncells) for c, m in zip(test, meshes)]
@@ -77,6 +80,10 @@ def run(n_train=96, n_test=24, wall=(64, 192), radial=(32, 96), max_steps=200000
         "speedup_learned_vs_plain": round(t_plain / t_learn, 2),
         "surrogate_error": {"linf_rel": sur_inf, "l2_rel": sur_l2, "free_stream_linf_rel": fs_inf},
         "steps_per_case_plain": steps_p.tolist(),
+        "steps_per_case_learned": (l1 + l2).tolist(),
+        "steps_per_case_batched": (b1 + b2).tolist(),
+        "linf_per_case_batched": per_case(st_b, plain_states),
+        "linf_per_case_learned": per_case(st_l, plain_states),
     }
     return out
 

@@ -9,8 +9,9 @@ the solver itself produces; training and inference run on the GPU
 (fvs2d_gb300.mlp).
 
 The fast solve is the precision ladder on a batch: mixed precision until
-each case's RMS(dU_rho) reaches `switch` x its reference level (the FP32 flux
-floor lies near 5e-6 of it), then FP64 to `drop` x the reference level.
+each case's RMS(dU) reaches `switch` x its reference levels in every
+component (the FP32 flux floor lies near 5e-6 of them), then FP64 to `drop`
+x the reference levels.
 """
 from __future__ import annotations
 
@@ -70,12 +71,12 @@ def solve_ladder(meshes, opts_mixed, levels, switch=1e-5, drop=1e-10, max_steps=
 
 
 def reference_levels(cases, meshes):
-    """First-step RMS(dU_rho) of a free-stream start (the plain path's first
-    residual), one short FP64 batch step."""
+    """First-step RMS(dU) per component of a free-stream start (the plain
+    path's first residuals), [ncases][4], one FP64 batch step."""
     with Batch(meshes, [sweep.case_options(c, PREC_FP64) for c in cases]) as b:
         b.initialize_solution()
         norms, _ = b.steps(1)
-    return norms[:, 0, 0].copy()
+    return norms[:, 0, :].copy()
 
 
 class WarmStart:

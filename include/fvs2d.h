@@ -238,12 +238,13 @@ int fvs_batch_set_precision(fvs_batch* b, int32_t precision);
 int fvs_batch_set_barrier_budget(fvs_batch* b, double seconds);
 /* nsteps (<= 1024) steps of every case; norms [ncases][nsteps][4] or NULL */
 int fvs_batch_steps(fvs_batch* b, int32_t nsteps, double* norms, float* ms);
-/* steps until each case's RMS(dU_rho) <= drop x its first value; converged
- * cases leave the work lists.  steps_done [ncases]; first, last [ncases][4] */
+/* steps until each case's RMS(dU) <= drop x its first value in all four
+ * components; converged cases leave the work lists.  steps_done [ncases];
+ * first, last [ncases][4] */
 int fvs_batch_run_to_drop(fvs_batch* b, int32_t max_steps, double drop, int32_t chunk, int32_t* steps_done,
                           double* first, double* last, float* ms);
-/* the same with an absolute target per case: RMS(dU_rho) <= levels[c]
- * (a warm start judged on the threshold of a free-stream start) */
+/* the same with absolute targets: RMS(dU_k) <= levels[c][k] for k = 0..3
+ * (a warm start judged on the thresholds of a free-stream start) */
 int fvs_batch_run_to_level(fvs_batch* b, int32_t max_steps, const double* levels, int32_t chunk, int32_t* steps_done,
                            double* first, double* last, float* ms);
 

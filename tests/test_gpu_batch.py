@@ -116,7 +116,7 @@ def test_run_to_drop_per_case():
         b.initialize_solution()
         done, first, last, _ = b.run_to_drop(80, drop=0.3, chunk=9)
     for c in range(3):
-        hit = np.nonzero(log[c, :, 0] <= 0.3 * log[c, 0, 0])[0]
+        hit = np.nonzero(np.all(log[c] <= 0.3 * log[c, 0][None, :], axis=1))[0]
         want = int(hit[0]) + 1 if hit.size else 80
         assert done[c] == want, (c, done[c], want)
         assert np.allclose(first[c], log[c, 0], rtol=1e-12)
