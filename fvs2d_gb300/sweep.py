@@ -77,15 +77,18 @@ def free_stream_state(c: Case, ncells: int, gamma: float = 1.4) -> np.ndarray:
     return np.tile(np.array([rho, rho * u, rho * v, e]), (ncells, 1))
 
 
-def run_plain(cases, precision, max_steps, drop, starts=None, ref_levels=None, check_every=200, states=None):
+def run_plain(cases, precision, max_steps, drop, starts=None, ref_levels=None, check_every=200, states=None,
+              meshes=None):
     """One Solver per case, one after the other (the plain path).  Returns
-    per-case steps, wall seconds total, and the first-step residuals; the
-    final states are appended to `states` when a list is given."""
+    per-case steps, wall seconds total (mesh generation excluded when meshes
+    are given), and the first-step residuals; the final states are appended
+    to `states` when a list is given."""
     from .solver import Solver
     steps, firsts = [], []
+    meshes = meshes if meshes is not None else [None] * len(cases)
     t0 = time.perf_counter()
     for k, c in enumerate(cases):
-        with Solver(c.mesh(), case_options(c, precision)) as s:
+        with Solver(meshes[k] if meshes[k] is not None else c.mesh(), case_options(c, precision)) as s:
             s.initialize_solution()
             if starts is not None:
                 s.cvar = starts[k]

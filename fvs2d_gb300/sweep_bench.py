@@ -35,7 +35,7 @@ def run(n_train=96, n_test=24, wall=(64, 192), radial=(32, 96), max_steps=200000
     tm = [c.mesh() for c in train]
     t0 = time.perf_counter()
     lv = reference_levels(train, tm)
-    states, n1, n2, t_solve, _ = solve_ladder(tm, [sweep.case_options(c, PREC_MIXED) for c in train], lv, switch, drop,
+    states, n1, n2, t_solve, _ph = solve_ladder(tm, [sweep.case_options(c, PREC_MIXED) for c in train], lv, switch, drop,
                                               max_steps)
     X, Y = build_dataset(train, states)
     t1 = time.perf_counter()
@@ -52,11 +52,11 @@ def run(n_train=96, n_test=24, wall=(64, 192), radial=(32, 96), max_steps=200000
     levels = reference_levels(test, meshes)
     plain_states = []
     steps_p, t_plain, firsts = sweep.run_plain(test, PREC_FP64, max_steps, drop, ref_levels=levels, check_every=500,
-                                               states=plain_states)
-    st_b, b1, b2, t_batch, _ = solve_ladder(meshes, [sweep.case_options(c, PREC_MIXED) for c in test], levels, switch, drop,
+                                               states=plain_states, meshes=meshes)
+    st_b, b1, b2, t_batch, ph_b = solve_ladder(meshes, [sweep.case_options(c, PREC_MIXED) for c in test], levels, switch, drop,
                                             max_steps)
     starts = [ws.predict_state(c, m) for c, m in zip(test, meshes)]
-    st_l, l1, l2, t_learn, _ = solve_ladder(meshes, [sweep.case_options(c, PREC_MIXED) for c in test], levels, switch,
+    st_l, l1, l2, t_learn, ph_l = solve_ladder(meshes, [sweep.case_options(c, PREC_MIXED) for c in test], levels, switch,
                                             drop, max_steps, starts=starts)
 
     def err(a, b):
@@ -73,12 +73,15 @@ def run(n_train=96, n_test=24, wall=(64, 192), radial=(32, 96), max_steps=200000
         "cells_test": int(sum(m.ncells for m in meshes)),
         "plain_fp64": {"seconds": round(t_plain, 3), "steps_total": int(steps_p.sum())},
         "batched_ladder": {"seconds": round(t_batch, 3), "steps_mixed": int(b1.max()), "steps_fp64": int(b2.max()),
-                           "linf_vs_plain": err(st_b, plain_states)},
+                           "linf_vs_plain": err(st_b, plain_states),
+                           "phase_seconds": {k: round(v, 3) for k, v in ph_b.items()}},
         "learned_batched_ladder": {"seconds": round(t_learn, 3), "steps_mixed": int(l1.max()), "steps_fp64": int(l2.max()),
-                                   "linf_vs_plain": err(st_l, plain_states)},
+                                   "linf_vs_plain": err(st_l, plain_states),
+                                   "phase_seconds": {k: round(v, 3) for k, v in ph_l.items()}},
         "speedup_batched_vs_plain": round(t_plain / t_batch, 2),
         "speedup_learned_vs_plain": round(t_plain / t_learn, 2),
         "surrogate_error": {"linf_rel": sur_inf, "l2_rel": sur_l2, "free_stream_linf_rel": fs_inf},
+        "cases": [[c.nw, c.nr, round(c.mach, 4), round(c.aoa, 3)] for c in test],
         "steps_per_case_plain": steps_p.tolist(),
         "steps_per_case_learned": (l1 + l2).tolist(),
         "steps_per_case_batched": (b1 + b2).tolist(),

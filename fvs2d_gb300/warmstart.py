@@ -51,23 +51,29 @@ def targets(case: sweep.Case, cvar: np.ndarray) -> np.ndarray:
 def solve_ladder(meshes, opts_mixed, levels, switch=1e-5, drop=1e-10, max_steps=200000, chunk=200, starts=None,
                  autotune=True):
     """Batched precision-ladder solve to levels*drop (levels: per-case
-    reference residuals).  Returns (states, steps_mixed, steps_fp64, seconds)."""
+    reference residuals [ncases][4]).  Returns (states, steps_mixed,
+    steps_fp64, seconds, phase seconds {setup, tune, mixed, fp64})."""
     t0 = time.perf_counter()
+    phases = {}
     with Batch(meshes, opts_mixed) as b:
         b.initialize_solution()
         if starts is not None:
             for c, u in enumerate(starts):
                 b.set_state(c, u)
+        t1 = time.perf_counter()
+        phases["setup"] = t1 - t0
         if autotune:
             b.autotune(2)
-            if starts is not None:
-                for c, u in enumerate(starts):
-                    b.set_state(c, u)
+        t2 = time.perf_counter()
+        phases["tune"] = t2 - t1
         n1, _, _, _ = b.run_to_level(max_steps, np.asarray(levels) * switch, chunk)
+        t3 = time.perf_counter()
+        phases["mixed"] = t3 - t2
         b.set_precision(PREC_FP64)
         n2, _, last, _ = b.run_to_level(max_steps, np.asarray(levels) * drop, chunk)
+        phases["fp64"] = time.perf_counter() - t3
         states = [b.get_state(c) for c in range(b.ncases)]
-    return states, n1, n2, time.perf_counter() - t0, last
+    return states, n1, n2, time.perf_counter() - t0, phases
 
 
 def reference_levels(cases, meshes):
