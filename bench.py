@@ -190,11 +190,8 @@ def run_ours(args) -> dict:
     barrier()
     clocks = clk.stop()
     t = ms / 1e3
-    if ws > 1:
-        tt = torch.tensor([t], dtype=torch.float64, device="cuda")
-        tdist.all_reduce(tt, op=tdist.ReduceOp.MAX)
-        t = float(tt.item())
-    value = ws * nc * nst * args.steps / t
+    t = max_over_ranks(t, "cuda")
+    value = whole_job_value(ws, nc * nst * args.steps, t)
 
     # per-kernel timing of one step (CUDA events on the library stream)
     prof = {}
@@ -260,6 +257,24 @@ def run_ours(args) -> dict:
     if ws > 1:
         tdist.destroy_process_group()
     return out if rank == 0 else None
+
+
+def max_over_ranks(seconds: float, device: str) -> float:
+    """The slowest rank's time (every rank gets it); the time itself when no
+    process group is initialised or it has one rank."""
+    import torch
+    import torch.distributed as tdist
+    if not (tdist.is_available() and tdist.is_initialized()) or tdist.get_world_size() == 1:
+        return seconds
+    tt = torch.tensor([seconds], dtype=torch.float64, device=device)
+    tdist.all_reduce(tt, op=tdist.ReduceOp.MAX)
+    return float(tt.item())
+
+
+def whole_job_value(world_size: int, units_per_rank: float, seconds: float) -> float:
+    """Whole-job throughput of independent replicas: every rank processes the
+    same number of units, the job takes the slowest rank's time."""
+    return world_size * units_per_rank / seconds
 
 
 def host_threads() -> int:

@@ -80,6 +80,7 @@ SIGNATURES = {
     "fvs_run_to_drop": (C.c_int, [C.c_void_p, C.c_double, C.c_int32, C.c_double, C.c_int32, C.POINTER(C.c_int32),
                                   C.c_void_p]),
     "fvs_vortex_error": (C.c_int, [C.c_void_p, C.c_double, C.c_void_p]),
+    "fvs_wall_loads": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p]),
     "fvs_mms_source": (C.c_int, [C.c_void_p, C.c_void_p]),
     "fvs_steps_device": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_float)]),
     "fvs_profile_step": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_int32), C.c_char_p, C.POINTER(C.c_float)]),

@@ -47,6 +47,56 @@ __global__ void k_gather_out_t(const T* __restrict__ dev, const int* __restrict_
   for (int k = 0; k < width; k++) ref[(size_t)width * i + k] = double(dev[(size_t)width * perm[i] + k]);
 }
 
+// Wall pressure coefficient, normal velocity and loads of one slip-wall
+// boundary (write_inst_cp_un, src/io.f90:340-446).  One block: every thread
+// evaluates the face values of its edges into `edges` [n][4] = (xf, cp,
+// cp_cell, un); thread 0 then sums in edge order into sums[7] = (cn, ca, cn1,
+// ca1, |un|max, sum un^2, sum |un|).  __dmul_rn / __dadd_rn / __dsub_rn round
+// each product and sum on its own (no multiply-add contraction), in the
+// reference's evaluation order.
+template <typename T>
+__global__ void k_wall_loads(DevView d, int g0, int n, double c2, double p_inf, double* edges, double* sums) {
+  const T* P = static_cast<const T*>(d.Pv);
+  const T* GX = static_cast<const T*>(d.Gx);
+  const T* GY = static_cast<const T*>(d.Gy);
+  const T* DL = static_cast<const T*>(d.edL);
+  const T* NR = static_cast<const T*>(d.enrm);
+  const T* AR = static_cast<const T*>(d.earea);
+  const T* XY = static_cast<const T*>(d.exy);
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const int g = g0 + i, c = d.ecell[g].x;
+    const double dx = double(DL[2 * g]), dy = double(DL[2 * g + 1]);
+    double w[4];
+    for (int v = 1; v < 4; v++)
+      w[v] = __dadd_rn(__dadd_rn(double(P[4 * c + v]), __dmul_rn(dx, double(GX[4 * c + v]))),
+                       __dmul_rn(dy, double(GY[4 * c + v])));
+    const double nx = double(NR[2 * g]), ny = double(NR[2 * g + 1]);
+    double* e = edges + 4 * (size_t)i;
+    e[0] = double(XY[2 * g]);
+    e[1] = __dmul_rn(c2, __dsub_rn(w[3], p_inf));
+    e[2] = __dmul_rn(c2, __dsub_rn(double(P[4 * c + 3]), p_inf));
+    e[3] = __dadd_rn(__dmul_rn(w[1], nx), __dmul_rn(w[2], ny));
+  }
+  __syncthreads();
+  if (threadIdx.x != 0) return;
+  double cn = 0, ca = 0, cn1 = 0, ca1 = 0, un_max = 0, un_l2 = 0, un_l1 = 0;
+  for (int i = 0; i < n; i++) {
+    const int g = g0 + i;
+    const double* e = edges + 4 * (size_t)i;
+    const double nx = double(NR[2 * g]), ny = double(NR[2 * g + 1]), af = double(AR[g]);
+    cn = __dadd_rn(cn, __dmul_rn(__dmul_rn(e[1], ny), af));
+    ca = __dadd_rn(ca, __dmul_rn(__dmul_rn(e[1], nx), af));
+    cn1 = __dadd_rn(cn1, __dmul_rn(__dmul_rn(e[2], ny), af));
+    ca1 = __dadd_rn(ca1, __dmul_rn(__dmul_rn(e[2], nx), af));
+    const double a = fabs(e[3]);
+    un_l2 = __dadd_rn(un_l2, __dmul_rn(e[3], e[3]));
+    un_l1 = __dadd_rn(un_l1, a);
+    un_max = un_max > a ? un_max : a;
+  }
+  sums[0] = cn; sums[1] = ca; sums[2] = cn1; sums[3] = ca1;
+  sums[4] = un_max; sums[5] = un_l2; sums[6] = un_l1;
+}
+
 }  // namespace
 
 struct fvs_handle {
@@ -72,8 +122,11 @@ struct fvs_handle {
   int nblk = 0;
   int launches_per_step = 0;
   bool host_only = false;
+  double* d_wall = nullptr;  // wall-load scratch, allocated on first use
+  size_t wall_cap = 0;
 
   ~fvs_handle() {
+    if (d_wall) cudaFree(d_wall);
     if (graph) cudaGraphExecDestroy(graph);
     if (ev0) cudaEventDestroy(ev0);
     if (ev1) cudaEventDestroy(ev1);
@@ -403,6 +456,9 @@ int fvs_init_state(fvs_handle* h) {
   if (h && h->host_only) return h->fail(FVS_ERR_INVALID, "host-only handle (fvs_create_host) has no device state");
   if (!h) return FVS_ERR_INVALID;
   // initialize_solution, src/initialize.f90:19-90 (ntstart <= 1)
+  if (h->o.ntstart > 1)
+    return h->fail(FVS_ERR_INVALID, "ntstart > 1 restarts from continuation files (src/initialize.f90:56-77): "
+                                    "read them on the host and call fvs_set_state");
   const int nc = h->hm.nc;
   std::vector<double> cv(4 * (size_t)nc);
   const double g = h->o.gamma, t0 = double(h->o.ntstart - 1) * h->o.dt;
@@ -568,6 +624,57 @@ int fvs_vortex_error(fvs_handle* h, double time, double* e) {
   const double n = double(m.cell_intr.size());
   for (int v = 0; v < 4; v++) { e[3 * v] = mx[v]; e[3 * v + 1] = l1[v] / n; e[3 * v + 2] = std::sqrt(l2[v] / n); }
   e[12] = std::sqrt(L2 / n);
+  return FVS_OK;
+}
+
+int fvs_wall_loads(fvs_handle* h, int32_t ib, double* edge_out, double* loads) {
+  if (h && h->host_only) return h->fail(FVS_ERR_INVALID, "host-only handle (fvs_create_host) has no device state");
+  if (!h || !loads) return FVS_ERR_INVALID;
+  const HostMesh& m = h->hm;
+  if (ib < 1 || ib > m.nb) return h->fail(FVS_ERR_INVALID, "boundary index out of range");
+  if (m.b_type[ib - 1] != FVS_BC_SLIP_WALL) return h->fail(FVS_ERR_INVALID, "wall loads need a slip_wall boundary");
+  const int n = m.b_eptr[ib] - m.b_eptr[ib - 1];
+  if (n <= 0) return h->fail(FVS_ERR_INVALID, "boundary has no edges");
+  if (m.st_ptr.empty()) return h->fail(FVS_ERR_INVALID, "no gradient operator");
+  const size_t need = 4 * (size_t)n + 8;
+  if (need > h->wall_cap) {
+    if (h->d_wall) cudaFree(h->d_wall);
+    h->d_wall = nullptr;
+    h->wall_cap = 0;
+    cudaError_t e = cudaMalloc(&h->d_wall, sizeof(double) * need);
+    if (e != cudaSuccess) return h->cuda_fail(e, "wall-load scratch");
+    h->wall_cap = need;
+  }
+  // gradient_cellcntr_1var (src/gradient.f90:75-96): the configured gradient
+  // without limiter, of the current state, also for first-order runs
+  DevView g = h->d;
+  g.first_order = 0;
+  g.limiter = FVS_LIM_NONE;
+  h->ks->cvar2pvar(h->d, h->stream);
+  h->ks->gradient(g, h->stream);
+  const double mach = h->o.mach_inf, c2 = 2.0 / (mach * mach);
+  const int g0 = h->d.nint + m.b_eptr[ib - 1];
+  double* sums = h->d_wall + 4 * (size_t)n;
+  if (h->mixed) k_wall_loads<float><<<1, 256, 0, h->stream>>>(h->d, g0, n, c2, h->pvar_inf[3], h->d_wall, sums);
+  else k_wall_loads<double><<<1, 256, 0, h->stream>>>(h->d, g0, n, c2, h->pvar_inf[3], h->d_wall, sums);
+  int rc = check_launch(h, "wall-load kernels");
+  if (rc) return rc;
+  double s[7];
+  cudaError_t e = cudaMemcpyAsync(s, sums, sizeof s, cudaMemcpyDeviceToHost, h->stream);
+  if (e == cudaSuccess && edge_out)
+    e = cudaMemcpyAsync(edge_out, h->d_wall, sizeof(double) * 4 * (size_t)n, cudaMemcpyDeviceToHost, h->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+  if (e != cudaSuccess) return h->cuda_fail(e, "wall-load download");
+  const double un_l2 = std::sqrt(s[5] / double(n)), un_l1 = s[6] / double(n);
+  // cosd / sind of the angle of attack in degrees
+  const double a = h->o.aoa_inf_deg * 3.141592653589793238462643383279502884 / 180.0;
+  const double ca = std::cos(a), sa = std::sin(a);
+  loads[0] = s[0] * ca - s[1] * sa;
+  loads[1] = s[0] * sa + s[1] * ca;
+  loads[2] = s[2] * ca - s[3] * sa;
+  loads[3] = s[2] * sa + s[3] * ca;
+  loads[4] = s[4]; loads[5] = un_l2; loads[6] = un_l1;
+  loads[7] = s[0]; loads[8] = s[1]; loads[9] = s[2]; loads[10] = s[3];
   return FVS_OK;
 }
 

@@ -71,8 +71,20 @@ class Solver:
         self.close()
 
     # -- state --------------------------------------------------------------
-    def initialize_solution(self) -> None:
+    def initialize_solution(self, cont_dir: str = ".") -> None:
+        """Free stream / vortex / MMS start (ntstart <= 1), or a restart from
+        cont.cd + cont.s8 in `cont_dir` (ntstart > 1, src/initialize.f90:56-77)."""
+        if self.options.ntstart > 1:
+            from . import ios
+            self.cvar = ios.read_cont(cont_dir, self.ncells, self.mesh.nnodes)
+            return
         self._check(self._lib.fvs_init_state(self._h))
+
+    def write_save(self, directory: str, ntimes: int, imach: int = 2) -> tuple[str, str]:
+        """save.cd + save.s8 of the current state (write_save_ios,
+        src/io.f90:93-114,156-178); ntimes = steps computed in this run."""
+        from . import ios
+        return ios.write_save(directory, self.cvar, self.mesh.nnodes, self.options.ntstart, ntimes, imach=imach)
 
     @property
     def cvar(self) -> np.ndarray:
@@ -149,6 +161,30 @@ class Solver:
         self._check(self._lib.fvs_vortex_error(self._h, float(time), capi.ptr(e)))
         return e
 
+    def wall_loads(self, ib: int = 1) -> tuple[np.ndarray, dict]:
+        """Wall pressure and loads of slip-wall boundary ib (1-based), the
+        numbers of write_inst_cp_un (src/io.f90:340-446): the edge table
+        [nedges][4] = (x_face, cp_wall, cp_cell, un) and a dict of cl, cd,
+        cl1, cd1, un_max, un_l2, un_l1, cn, ca, cn1, ca1."""
+        n = int(self.mesh.bndry_cells[ib - 1].size) if 1 <= ib <= len(self.mesh.bndry_cells) else 0
+        e = np.empty((max(n, 1), 4), np.float64)
+        loads = np.empty(11, np.float64)
+        self._check(self._lib.fvs_wall_loads(self._h, int(ib), capi.ptr(e), capi.ptr(loads)))
+        return e[:n], dict(zip(WALL_LOAD_NAMES, loads.tolist()))
+
+    def write_cp(self, path: str, ib: int = 1, sol_time: float = 0.0) -> dict:
+        """One zone of the reference's Tecplot cp file (x, cp_w, cp_cell per
+        wall edge, src/io.f90:387-409); returns the loads."""
+        e, loads = self.wall_loads(ib)
+        with open(path, "w") as f:
+            f.write('TITLE     = "cp"\n')
+            f.write('VARIABLES = "x" "cp_w" "cp_cell"\n')
+            f.write(f"ZONE I={e.shape[0]} J=1\n")
+            f.write(f"STRANDID=1, SOLUTIONTIME={_e16(sol_time)}\n")
+            for xf, cp, cp1, _ in e:
+                f.write(f"{_e16(xf)} {_e16(cp)} {_e16(cp1)} \n")
+        return loads
+
     def mms_source(self) -> np.ndarray:
         s = np.empty((self.ncells, 4), np.float64)
         self._check(self._lib.fvs_mms_source(self._h, capi.ptr(s)))
@@ -163,6 +199,19 @@ class Solver:
         if n.value:
             self._check(self._lib.fvs_export(self._h, name.encode(), capi.ptr(out), n.value))
         return out[: n.value // np.dtype(dtype).itemsize]
+
+
+WALL_LOAD_NAMES = ("cl", "cd", "cl1", "cd1", "un_max", "un_l2", "un_l1", "cn", "ca", "cn1", "ca1")
+
+
+def _e16(x: float) -> str:
+    """Fortran e16.8: 0.dddddddd E+xx, right-justified in 16 columns."""
+    if not np.isfinite(x):
+        return f"{x!s:>16}"
+    if x == 0.0:
+        return "0.00000000E+00".rjust(16)
+    mant, ex = f"{abs(x):.7E}".split("E")
+    return (("-" if x < 0 else "") + f"0.{mant.replace('.', '')}E{int(ex) + 1:+03d}").rjust(16)
 
 
 INT_EXPORTS = {"cell_nghbr", "cell_nghbre", "cell_edge", "edge_nodes", "edge_cells", "edge_intr", "edge_bndr",

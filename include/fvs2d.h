@@ -165,7 +165,9 @@ int fvs_export_size(const fvs_handle* h, const char* name, int64_t* nbytes);
 int fvs_export(const fvs_handle* h, const char* name, void* dst, int64_t nbytes);
 
 /* initialize_solution (src/initialize.f90:19-90) for ntstart <= 1:
- * free stream, exact vortex at t=(ntstart-1)*dt, or MMS. */
+ * free stream, exact vortex at t=(ntstart-1)*dt, or MMS.  ntstart > 1 (a
+ * restart from the cont.cd / cont.s8 files, src/initialize.f90:56-77) returns
+ * FVS_ERR_INVALID: the host reads the files and calls fvs_set_state. */
 int fvs_init_state(fvs_handle* h);
 int fvs_set_state(fvs_handle* h, const double* cvar);   /* [ncells][4] */
 int fvs_get_state(fvs_handle* h, double* cvar);         /* [ncells][4] */
@@ -187,6 +189,15 @@ int fvs_time_integration(fvs_handle* h, double t1, int32_t nsteps, double* resno
  * (steps run as captured CUDA graphs in between). */
 int fvs_run_to_drop(fvs_handle* h, double t1, int32_t max_steps, double drop,
                     int32_t check_every, int32_t* steps_done, double* resnorm);
+
+/* Wall pressure and loads of slip-wall boundary ib (1-based), the numbers
+ * write_inst_cp_un writes (src/io.f90:340-446).  Face values use the
+ * configured cell-centre gradient of the current state without limiter
+ * (gradient_cellcntr_1var, src/gradient.f90:75-96), also for first-order
+ * runs.  edge_out [nedges][4] = (x_face, cp_wall, cp_cell, un) in the
+ * boundary's edge order, or NULL; loads[11] = cl, cd, cl1, cd1, |Vn|max,
+ * |Vn|_2, |Vn|_1, cn, ca, cn1, ca1 (the "1" values use the cell pressure). */
+int fvs_wall_loads(fvs_handle* h, int32_t ib, double* edge_out, double* loads);
 
 /* error_isentropic_vortex (src/mms.f90:271-365): the 13 numbers of one
  * log_vortex_err.plt row after the time column. */

@@ -1625,6 +1625,58 @@ int orc_get_gradient(const orc* c, double* grad, double* phi) {
   return FVS_OK;
 }
 
+/* write_inst_cp_un, src/io.f90:340-446: wall pressure coefficient and loads
+ * of boundary ib (1-based, slip_wall).  The face values use the cell-centre
+ * gradients of p, u, v from gradient_cellcntr_1var (src/gradient.f90:75-96),
+ * the configured gradient without limiter, computed also for first-order
+ * runs; the 1-variable routines (src/gradient_lsq.f90:425-441,
+ * src/gradient_ggcb.f90:144-166, src/gradient_ggnb.f90:216-243) do the same
+ * arithmetic per variable as gradient_cell.  edge_out [nedges][4] =
+ * (xf, cp, cp_cell, un) in edge order (may be NULL); loads[11] = cl, cd, cl1,
+ * cd1, |Vn|max, |Vn|_2, |Vn|_1, cn, ca, cn1, ca1. */
+int orc_wall_loads(orc* c, int ib, double* edge_out, double* loads) {
+  if (ib < 1 || ib > c->nb || c->b_type[ib] != FVS_BC_SLIP_WALL || !loads) return FVS_ERR_INVALID;
+  for (int ic = 1; ic <= c->ncells; ic++) cvar2pvar_cell(c, ic);
+  for (int ic = 1; ic <= c->ncells; ic++) gradient_cell(c, ic);
+  const double m = c->o.mach_inf, p_inf = c->pvar_inf[3];
+  const int n = c->b_nedges[ib];
+  double un_max = 0.0, un_l2 = 0.0, un_l1 = 0.0, cn = 0.0, ca = 0.0, cn1 = 0.0, ca1 = 0.0;
+  for (int i = 1; i <= n; i++) {
+    int ie = c->b_edge[c->b_eptr[ib] + i];
+    int ic = c->b_cell[c->b_cptr[ib] + i - 1];
+    double xf = c->ex[ie], af = c->ea[ie], nx = c->enx[ie], ny = c->eny[ie];
+    double dx = mix(c, c->ex[ie] - c->xc[ic]), dy = miy(c, c->ey[ie] - c->yc[ic]);
+    double pw = P(c, ic, 3) + dx * G(c, ic, 3, 0) + dy * G(c, ic, 3, 1);
+    double cp = 2.0 / (m * m) * (pw - p_inf);
+    double cp1 = 2.0 / (m * m) * (P(c, ic, 3) - p_inf);
+    cn = cn + cp * ny * af;
+    ca = ca + cp * nx * af;
+    cn1 = cn1 + cp1 * ny * af;
+    ca1 = ca1 + cp1 * nx * af;
+    double uw = P(c, ic, 1) + dx * G(c, ic, 1, 0) + dy * G(c, ic, 1, 1);
+    double vw = P(c, ic, 2) + dx * G(c, ic, 2, 0) + dy * G(c, ic, 2, 1);
+    double un = uw * nx + vw * ny;
+    un_l2 = un_l2 + un * un;
+    un_l1 = un_l1 + fabs(un);
+    un_max = un_max > fabs(un) ? un_max : fabs(un);
+    if (edge_out) {
+      double* e = edge_out + 4 * (size_t)(i - 1);
+      e[0] = xf; e[1] = cp; e[2] = cp1; e[3] = un;
+    }
+  }
+  un_l2 = sqrt(un_l2 / (double)n);
+  un_l1 = un_l1 / (double)n;
+  /* cosd / sind of the angle of attack in degrees */
+  const double a = c->o.aoa_inf_deg * PI / 180.0, ca_ = cos(a), sa = sin(a);
+  loads[0] = cn * ca_ - ca * sa;
+  loads[1] = cn * sa + ca * ca_;
+  loads[2] = cn1 * ca_ - ca1 * sa;
+  loads[3] = cn1 * sa + ca1 * ca_;
+  loads[4] = un_max; loads[5] = un_l2; loads[6] = un_l1;
+  loads[7] = cn; loads[8] = ca; loads[9] = cn1; loads[10] = ca1;
+  return FVS_OK;
+}
+
 /* error_isentropic_vortex, src/mms.f90:271-365 */
 int orc_vortex_error(orc* c, double time, double* e) {
   double g = c->o.gamma;

@@ -39,6 +39,7 @@ int  orc_get_state(const orc* c, double* cvar);
  * reference's summation order) that gives bit-identical results. */
 int  orc_residual(orc* c, double time, double* resid, double* ws, int nthreads);
 int  orc_get_gradient(const orc* c, double* grad, double* phi);
+int  orc_wall_loads(orc* c, int ib, double* edge_out, double* loads);
 int  orc_time_integration(orc* c, double t1, int nsteps, double* resnorm, int nthreads);
 int  orc_vortex_error(orc* c, double time, double* err13);
 int  orc_mms_source(const orc* c, double* src);

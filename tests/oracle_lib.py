@@ -16,7 +16,7 @@ sys.path.insert(0, ROOT)
 sys.path.insert(0, os.path.join(ROOT, "oracle"))
 
 from fvs2d_gb300 import capi  # noqa: E402
-from fvs2d_gb300.solver import INT_EXPORTS  # noqa: E402
+from fvs2d_gb300.solver import INT_EXPORTS, WALL_LOAD_NAMES  # noqa: E402
 
 import build_oracle  # noqa: E402
 
@@ -39,6 +39,7 @@ def load() -> C.CDLL:
             "orc_get_state": (C.c_int, [vp, vp]),
             "orc_residual": (C.c_int, [vp, C.c_double, vp, vp, C.c_int]),
             "orc_get_gradient": (C.c_int, [vp, vp, vp]),
+            "orc_wall_loads": (C.c_int, [vp, C.c_int, vp, vp]),
             "orc_time_integration": (C.c_int, [vp, C.c_double, C.c_int, vp, C.c_int]),
             "orc_vortex_error": (C.c_int, [vp, C.c_double, vp]),
             "orc_mms_source": (C.c_int, [vp, vp]),
@@ -113,6 +114,16 @@ class Oracle:
         p = np.empty(self.ncells)
         self._lib.orc_get_gradient(self._h, capi.ptr(g), capi.ptr(p))
         return g, p
+
+    def wall_loads(self, ib=1, n_edges=None):
+        """(edge table [n][4] = xf, cp, cp_cell, un; loads dict) of boundary ib."""
+        loads = np.empty(11)
+        n = n_edges if n_edges is not None else 0
+        e = np.empty((max(n, 1), 4))
+        rc = self._lib.orc_wall_loads(self._h, int(ib), capi.ptr(e) if n else None, capi.ptr(loads))
+        if rc:
+            raise OracleError(rc, "wall_loads")
+        return e[:n], dict(zip(WALL_LOAD_NAMES, loads))
 
     def time_integration(self, t1, nsteps):
         out = np.empty((max(nsteps, 1), 4))
