@@ -102,14 +102,17 @@ class Batch:
                                                     capi.ptr(first), capi.ptr(last), C.byref(ms)))
         return done, first, last, ms.value
 
-    def run_to_level(self, max_steps: int, levels, chunk: int = 50):
-        """Steps until each case's RMS(dU_k) <= levels[c, k] for all k; same returns as run_to_drop."""
+    def run_to_level(self, max_steps: int, levels, chunk: int = 50, dc: bool = False):
+        """Steps until each case's RMS(dU_k) <= levels[c, k] for all k; same
+        returns as run_to_drop.  dc: defect-correction iteration (first-order
+        steady batches; leaves the batch in FP64)."""
         lv = np.ascontiguousarray(np.broadcast_to(np.asarray(levels, np.float64).reshape(self.ncases, -1),
                                                   (self.ncases, 4)), np.float64)
         done = np.zeros(self.ncases, np.int32)
         first = np.zeros((self.ncases, 4))
         last = np.zeros((self.ncases, 4))
         ms = C.c_float(0)
-        self._check(self._lib.fvs_batch_run_to_level(self._h, int(max_steps), capi.ptr(lv), int(chunk), capi.ptr(done),
-                                                     capi.ptr(first), capi.ptr(last), C.byref(ms)))
+        fn = self._lib.fvs_batch_run_to_level_dc if dc else self._lib.fvs_batch_run_to_level
+        self._check(fn(self._h, int(max_steps), capi.ptr(lv), int(chunk), capi.ptr(done), capi.ptr(first),
+                       capi.ptr(last), C.byref(ms)))
         return done, first, last, ms.value

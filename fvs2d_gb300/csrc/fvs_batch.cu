@@ -104,6 +104,7 @@ struct fvs_batch {
   bool plan_dirty = true, use_graph = true;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   int* h_step0 = nullptr;
+  DcView dc;  // defect-correction arrays, allocated on first use
 
   ~fvs_batch() {
     if (graph) cudaGraphExecDestroy(graph);
@@ -328,6 +329,28 @@ int launch_chunk(fvs_batch* B, int nsteps, int step0) {
     if (e == cudaSuccess) e = B->ks->persistent(B->d, B->plan, grid, B->block, B->stream);
     if (e != cudaSuccess) return B->cuda_fail(e, "persistent launch");
   }
+  return FVS_OK;
+}
+
+// View of precision prec: the current one, or a variant built on first use
+// from the stored host meshes (same device order as every other variant).
+int variant_view(fvs_batch* B, int prec, DevView** out) {
+  if (prec == B->prec) {
+    *out = &B->d;
+    return FVS_OK;
+  }
+  fvs_batch::Variant& v = B->var[prec];
+  if (!v.built) {
+    init_view_constants(B, v.d);
+    const int cur = B->prec;  // build_batch_device reads the precision
+    B->prec = prec;
+    int rc = prec == FVS_PREC_MIXED ? build_batch_device<float>(B, v.d) : build_batch_device<double>(B, v.d);
+    B->prec = cur;
+    if (rc) return rc;
+    v.built = true;
+    v.block = B->block; v.tile = B->tile; v.bps = B->bps;
+  }
+  *out = &v.d;
   return FVS_OK;
 }
 
@@ -644,6 +667,111 @@ static int run_until(fvs_batch* b, int32_t max_steps, double drop, const double*
   cudaEventRecord(b->ev1, b->stream);
   cudaEventSynchronize(b->ev1);
   if (ms) cudaEventElapsedTime(ms, b->ev0, b->ev1);
+  std::fill(b->active.begin(), b->active.end(), 1);
+  b->plan_dirty = true;
+  if (steps_done) std::memcpy(steps_done, done.data(), 4 * (size_t)nc);
+  if (first) std::memcpy(first, f.data(), 32 * (size_t)nc);
+  if (last) std::memcpy(last, l.data(), 32 * (size_t)nc);
+  if (rc) return rc;
+  return nonfinite ? b->fail(FVS_ERR_NONFINITE, "a case's residual norm is not finite") : FVS_OK;
+}
+
+// Defect-correction run of a first-order steady batch to absolute per-case
+// levels [ncases][4].  Each chunk of `chunk` steps: fold the correction into
+// the FP64 state, evaluate the FP64 residual and local dt there, then iterate
+// the correction in one cooperative launch with the linearised residual.
+// The norms are the RMS of the correction increments per step.  Leaves the
+// batch in FP64 with the folded state.
+int fvs_batch_run_to_level_dc(fvs_batch* b, int32_t max_steps, const double* levels, int32_t chunk,
+                              int32_t* steps_done, double* first, double* last, float* ms) {
+  if (!b || !levels || max_steps <= 0 || chunk <= 0 || chunk > b->norm_cap) return FVS_ERR_INVALID;
+  if (!b->base.steady || b->base.reconst != FVS_RECON_UPWIND1)
+    return b->fail(FVS_ERR_INVALID, "defect correction runs first-order steady batches");
+  int rc = fvs_batch_set_precision(b, FVS_PREC_FP64);
+  if (rc) return rc;
+  DevView* d32 = nullptr;
+  if ((rc = variant_view(b, FVS_PREC_MIXED, &d32))) return rc;
+  DevView& d64 = b->d;
+  const size_t n4 = 16 * (size_t)b->nc;
+  if (!b->dc.D) {
+    void* p[5];
+    for (int k = 0; k < 5; k++)
+      if (!b->arena.alloc(p[k], n4)) return b->fail(FVS_ERR_NOMEM, "defect-correction arrays");
+    b->dc.D = static_cast<float*>(p[0]); b->dc.D0 = static_cast<float*>(p[1]);
+    b->dc.DF = static_cast<float*>(p[2]); b->dc.dP = static_cast<float*>(p[3]);
+    b->dc.R0 = static_cast<float*>(p[4]);
+  }
+  cudaError_t e = cudaMemsetAsync(b->dc.D, 0, n4, b->stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(b->dc.dP, 0, n4, b->stream);
+  if (e != cudaSuccess) return b->cuda_fail(e, "defect-correction reset");
+  const DcKernels& K = dc_kernels();
+  const KernelSet& K64 = kernels_fp64_fast();
+  // launch shape of the mixed variant (tuned there when the batch ran mixed)
+  const fvs_batch::Variant& vm = b->var[FVS_PREC_MIXED];
+  const int sb = b->block, st = b->tile, sp = b->bps;
+  if (vm.built) { b->block = vm.block; b->tile = vm.tile; b->bps = vm.bps; }
+  const int occ = K.occupancy(b->block);
+  if (occ <= 0) return b->fail(FVS_ERR_INVALID, "no resident block for the defect-correction kernel");
+  const int grid = std::max(1, std::min(b->bps, occ)) * b->nsm;
+  const int nc = b->ncases;
+  std::vector<double> f(4 * (size_t)nc, -1.0), l(4 * (size_t)nc, 0.0);
+  std::vector<int> done(nc, max_steps);
+  std::fill(b->active.begin(), b->active.end(), 1);
+  b->plan_dirty = true;
+  std::vector<double> all(4 * (size_t)nc * b->norm_cap);
+  cudaEventRecord(b->ev0, b->stream);
+  int step = 0;
+  bool nonfinite = false;
+  while (step < max_steps) {
+    const int n = std::min(chunk, max_steps - step);
+    if (b->plan_dirty && (rc = build_plan(b))) break;
+    // base state of the chunk: fold, FP64 residual and wave speeds, FP32 copies
+    K.fold(*d32, b->dc, d64.U, b->stream);
+    K64.cvar2pvar(d64, b->stream);
+    K64.flux(d64, 0.0, b->stream);
+    K64.residual_out(d64, b->stream);
+    K.base(*d32, b->dc, d64.U, d64.resid, d64.ws, b->stream);
+    *b->h_step0 = step;
+    e = cudaMemcpyAsync(b->d_step0, b->h_step0, sizeof(int), cudaMemcpyHostToDevice, b->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(b->d_bar, 0, sizeof(GridBarrier), b->stream);
+    b->plan.nsteps = n;
+    if (e == cudaSuccess) e = K.persistent(*d32, b->plan, b->dc, grid, b->block, b->stream);
+    if (e != cudaSuccess) { rc = b->cuda_fail(e, "defect-correction chunk"); break; }
+    if ((rc = check_barrier(b))) break;
+    e = cudaMemcpy(all.data(), b->d_case_norms, 8 * all.size(), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) { rc = b->cuda_fail(e, "norm download"); break; }
+    bool changed = false;
+    int nact = 0;
+    for (int c = 0; c < nc; c++) {
+      if (!b->active[c]) continue;
+      for (int s = 0; s < n; s++) {
+        const double* v = &all[4 * ((size_t)c * b->norm_cap + (step + s) % b->norm_cap)];
+        if (!std::isfinite(v[0])) { nonfinite = true; b->active[c] = 0; done[c] = step + s + 1; changed = true; break; }
+        if (f[4 * c] < 0) std::memcpy(&f[4 * c], v, 32);
+        std::memcpy(&l[4 * c], v, 32);
+        bool conv = true;
+        for (int k = 0; k < 4; k++) conv = conv && v[k] <= levels[4 * c + k];
+        if (conv) {
+          done[c] = step + s + 1;
+          b->active[c] = 0;
+          changed = true;
+          break;
+        }
+      }
+      nact += b->active[c];
+    }
+    step += n;
+    if (nact == 0) break;
+    if (changed) b->plan_dirty = true;
+  }
+  // the last correction into the FP64 state
+  K.fold(*d32, b->dc, d64.U, b->stream);
+  K64.cvar2pvar(d64, b->stream);
+  cudaEventRecord(b->ev1, b->stream);
+  e = cudaEventSynchronize(b->ev1);
+  if (!rc && e != cudaSuccess) rc = b->cuda_fail(e, "defect-correction run");
+  if (ms) cudaEventElapsedTime(ms, b->ev0, b->ev1);
+  b->block = sb; b->tile = st; b->bps = sp;
   std::fill(b->active.begin(), b->active.end(), 1);
   b->plan_dirty = true;
   if (steps_done) std::memcpy(steps_done, done.data(), 4 * (size_t)nc);

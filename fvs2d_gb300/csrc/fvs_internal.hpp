@@ -188,6 +188,32 @@ struct KernelSet {
   int (*persistent_occupancy)(const DevView&, int block);
   cudaError_t (*persistent)(const DevView&, const PersistPlan&, int grid, int block, cudaStream_t);
 };
+// Defect correction of a first-order steady batch (mixed build): per chunk
+// the FP64 residual R0 of the base state is evaluated once; the RK stages
+// then iterate a correction dU of the base with the linearised residual
+// R0 + J dU, J dU evaluated in FP32 by forward-mode differentiation of the
+// Roe flux.  Arrays are [nc][4] FP32 in device order.
+struct DcView {
+  float* D = nullptr;    // correction dU
+  float* D0 = nullptr;   // correction at the start of the step
+  float* DF = nullptr;   // stage accumulator (fcvar)
+  float* dP = nullptr;   // primitive tangent of dU at the base state
+  float* R0 = nullptr;   // FP64 residual of the base state, rounded to FP32
+};
+
+struct DcKernels {
+  // U64 += dU; dU = dP = 0 (all cells)
+  void (*fold)(const DevView& d32, const DcView& c, double* U64, cudaStream_t);
+  // FP32 primitives of the base, R0 from the FP64 residual, local dt from
+  // the FP64 wave speeds (all cells)
+  void (*base)(const DevView& d32, const DcView& c, const double* U64, const double* resid64, const double* ws64,
+               cudaStream_t);
+  int (*occupancy)(int block);
+  cudaError_t (*persistent)(const DevView& d32, const PersistPlan& p, const DcView& c, int grid, int block,
+                            cudaStream_t);
+};
+const DcKernels& dc_kernels();
+
 const KernelSet& kernels_fp64_strict();
 const KernelSet& kernels_fp64_fast();
 const KernelSet& kernels_mixed();

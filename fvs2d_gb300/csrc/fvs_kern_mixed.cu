@@ -14,4 +14,8 @@ const KernelSet& kernels_mixed() {
                               k_mixed::launch_persistent};
   return k;
 }
+const DcKernels& dc_kernels() {
+  static const DcKernels k = {k_mixed::dc_fold, k_mixed::dc_base, k_mixed::dc_occupancy, k_mixed::dc_persistent};
+  return k;
+}
 }  // namespace fvs

@@ -189,50 +189,57 @@ __device__ __forceinline__ void roe_flux(T gamma, const T* pl, const T* pr, T nx
 //  - the eigenvector sum drops the products with the constants 0 and 1
 // Differences to the source form are rounding-level (relative ~1e-16 per
 // operation), checked against the oracle at 1e-12.
+// R: the scalar type (T, or the FP32 dual number of the linearised residual)
+template <typename R>
+__device__ __forceinline__ void roe_flux_fast_t(R gamma, R gm1, R igm1, const R* pl, const R* pr, R nx, R ny, R* flux,
+                                                R& ws_max) {
+  const R tx = -ny, ty = nx;
+  const R rhoL = pl[0], uL = pl[1], vL = pl[2], pL = pl[3];
+  const R rhoR = pr[0], uR = pr[1], vR = pr[2], pR = pr[3];
+  const R riL = R(1) / rhoL, riR = R(1) / rhoR;
+  const R unL = uL * nx + vL * ny, unR = uR * nx + vR * ny;
+  const R utL = uL * tx + vL * ty, utR = uR * tx + vR * ty;
+  const R HL = gamma * pL * riL * igm1 + R(0.5) * (uL * uL + vL * vL);
+  const R HR = gamma * pR * riR * igm1 + R(0.5) * (uR * uR + vR * vR);
+  const R RT = dsqrt_(rhoR * riL);
+  const R rho = RT * rhoL;
+  const R i1 = R(1) / (R(1) + RT);
+  const R u = (uL + RT * uR) * i1;
+  const R v = (vL + RT * vR) * i1;
+  const R H = (HL + RT * HR) * i1;
+  const R q2 = R(0.5) * (u * u + v * v);
+  const R a2 = gm1 * (H - q2);
+  const R a = dsqrt_(a2);
+  const R ia2 = R(1) / a2;
+  const R un = u * nx + v * ny;
+  const R ut = u * tx + v * ty;
+  const R drho = rhoR - rhoL, dp = pR - pL, dun = unR - unL, dut = utR - utL;
+  const R rad = rho * a * dun;
+  const R L0 = (dp - rad) * R(0.5) * ia2;
+  const R L1 = rho * dut;
+  const R L2 = drho - dp * ia2;
+  const R L3 = (dp + rad) * R(0.5) * ia2;
+  R ws0 = dabs_(un - a), ws3 = dabs_(un + a);
+  const R ws1 = dabs_(un);
+  if (ws0 < R(0.2)) ws0 = R(0.5) * (ws0 * ws0 * R(5) + R(0.2));
+  if (ws3 < R(0.2)) ws3 = R(0.5) * (ws3 * ws3 * R(5) + R(0.2));
+  const R w0 = ws0 * L0, w1 = ws1 * L1, w2 = ws1 * L2, w3 = ws3 * L3;
+  const R s03 = w0 + w3, s = s03 + w2, dw = (w3 - w0) * a;
+  const R diss0 = s;
+  const R diss1 = u * s + dw * nx + w1 * tx;
+  const R diss2 = v * s + dw * ny + w1 * ty;
+  const R diss3 = H * s03 + un * dw + w1 * ut + w2 * q2;
+  const R mL = rhoL * unL, mR = rhoR * unR;
+  flux[0] = R(0.5) * (mL + mR - diss0);
+  flux[1] = R(0.5) * (mL * uL + mR * uR + (pL + pR) * nx - diss1);
+  flux[2] = R(0.5) * (mL * vL + mR * vR + (pL + pR) * ny - diss2);
+  flux[3] = R(0.5) * (mL * HL + mR * HR - diss3);
+  ws_max = R(0.5) * (ws1 + a);
+}
+
 __device__ __forceinline__ void roe_flux_fast(T gamma, T gm1, T igm1, const T* pl, const T* pr, T nx, T ny, T* flux,
                                               T& ws_max) {
-  const T tx = -ny, ty = nx;
-  const T rhoL = pl[0], uL = pl[1], vL = pl[2], pL = pl[3];
-  const T rhoR = pr[0], uR = pr[1], vR = pr[2], pR = pr[3];
-  const T riL = T(1) / rhoL, riR = T(1) / rhoR;
-  const T unL = uL * nx + vL * ny, unR = uR * nx + vR * ny;
-  const T utL = uL * tx + vL * ty, utR = uR * tx + vR * ty;
-  const T HL = gamma * pL * riL * igm1 + T(0.5) * (uL * uL + vL * vL);
-  const T HR = gamma * pR * riR * igm1 + T(0.5) * (uR * uR + vR * vR);
-  const T RT = dsqrt_(rhoR * riL);
-  const T rho = RT * rhoL;
-  const T i1 = T(1) / (T(1) + RT);
-  const T u = (uL + RT * uR) * i1;
-  const T v = (vL + RT * vR) * i1;
-  const T H = (HL + RT * HR) * i1;
-  const T q2 = T(0.5) * (u * u + v * v);
-  const T a2 = gm1 * (H - q2);
-  const T a = dsqrt_(a2);
-  const T ia2 = T(1) / a2;
-  const T un = u * nx + v * ny;
-  const T ut = u * tx + v * ty;
-  const T drho = rhoR - rhoL, dp = pR - pL, dun = unR - unL, dut = utR - utL;
-  const T rad = rho * a * dun;
-  const T L0 = (dp - rad) * T(0.5) * ia2;
-  const T L1 = rho * dut;
-  const T L2 = drho - dp * ia2;
-  const T L3 = (dp + rad) * T(0.5) * ia2;
-  T ws0 = dabs_(un - a), ws3 = dabs_(un + a);
-  const T ws1 = dabs_(un);
-  if (ws0 < T(0.2)) ws0 = T(0.5) * (ws0 * ws0 * T(5) + T(0.2));
-  if (ws3 < T(0.2)) ws3 = T(0.5) * (ws3 * ws3 * T(5) + T(0.2));
-  const T w0 = ws0 * L0, w1 = ws1 * L1, w2 = ws1 * L2, w3 = ws3 * L3;
-  const T s03 = w0 + w3, s = s03 + w2, dw = (w3 - w0) * a;
-  const T diss0 = s;
-  const T diss1 = u * s + dw * nx + w1 * tx;
-  const T diss2 = v * s + dw * ny + w1 * ty;
-  const T diss3 = H * s03 + un * dw + w1 * ut + w2 * q2;
-  const T mL = rhoL * unL, mR = rhoR * unR;
-  flux[0] = T(0.5) * (mL + mR - diss0);
-  flux[1] = T(0.5) * (mL * uL + mR * uR + (pL + pR) * nx - diss1);
-  flux[2] = T(0.5) * (mL * vL + mR * vR + (pL + pR) * ny - diss2);
-  flux[3] = T(0.5) * (mL * HL + mR * HR - diss3);
-  ws_max = T(0.5) * (ws1 + a);
+  roe_flux_fast_t<T>(gamma, gm1, igm1, pl, pr, nx, ny, flux, ws_max);
 }
 
 // ---------------------------------------------------------------------------
@@ -896,6 +903,244 @@ static void launch_update(const DevView& d, const StageParams& sp, cudaStream_t 
 
 static void launch_residual_out(const DevView& d, cudaStream_t s) { k_residual_out<<<grid_of(d.nc), 256, 0, s>>>(d); }
 static void launch_norm_final(const DevView& d, cudaStream_t s) { k_norm_final<<<1, 256, 0, s>>>(d); }
+
+#if FVS_MIXED
+// ---------------------------------------------------------------------------
+// defect correction (first-order steady batches)
+// ---------------------------------------------------------------------------
+// FP32 dual number (value, tangent): forward-mode derivative of the Roe flux,
+// i.e. the Jacobian-vector product J(U) dU of the linearised residual.
+struct Dual {
+  float v, d;
+  __device__ __forceinline__ Dual() {}
+  __device__ __forceinline__ Dual(float x) : v(x), d(0.f) {}
+  __device__ __forceinline__ Dual(float x, float dx) : v(x), d(dx) {}
+};
+__device__ __forceinline__ Dual operator+(Dual a, Dual b) { return Dual(a.v + b.v, a.d + b.d); }
+__device__ __forceinline__ Dual operator-(Dual a, Dual b) { return Dual(a.v - b.v, a.d - b.d); }
+__device__ __forceinline__ Dual operator-(Dual a) { return Dual(-a.v, -a.d); }
+__device__ __forceinline__ Dual operator*(Dual a, Dual b) { return Dual(a.v * b.v, a.d * b.v + a.v * b.d); }
+__device__ __forceinline__ Dual operator/(Dual a, Dual b) {
+  const float r = 1.0f / b.v, q = a.v * r;
+  return Dual(q, (a.d - q * b.d) * r);
+}
+__device__ __forceinline__ bool operator<(Dual a, Dual b) { return a.v < b.v; }
+__device__ __forceinline__ Dual dsqrt_(Dual a) {
+  const float s = sqrtf(a.v);
+  return Dual(s, 0.5f * a.d / s);
+}
+__device__ __forceinline__ Dual dabs_(Dual a) { return a.v < 0.f ? -a : a; }
+
+// J dU of one edge slot (first order: face states are the cell states),
+// times the face area, into the slot's flux record
+__device__ __forceinline__ void dc_flux_item(const DevView& d, const DcView& c, int e) {
+  const float* P = static_cast<const float*>(d.Pv);
+  const int2 lr = d.ecell[e];
+  const T2 n = ld2(d.enrm, e);
+  const float af = static_cast<const float*>(d.earea)[e];
+  float pl[4], ql[4], pr[4], qr[4];
+  ld4(P, lr.x, pl);
+  ldc4<true>(c.dP, lr.x, ql);
+  if (lr.y >= 0) {
+    ld4(P, lr.y, pr);
+    ldc4<true>(c.dP, lr.y, qr);
+  } else {
+    const int rec = d.ebtype[e];
+    const T2 xy = ld2(d.exy, e);
+    ghost_state(d, rec, 0.0, xy.x, xy.y, n.x, n.y, pl, pr);
+    if ((rec & 15) == FVS_BC_SLIP_WALL) {
+      // the mirror state is linear in the interior state
+      const float un = ql[1] * n.x + ql[2] * n.y;
+      qr[0] = ql[0];
+      qr[1] = ql[1] - 2.0f * un * n.x;
+      qr[2] = ql[2] - 2.0f * un * n.y;
+      qr[3] = ql[3];
+    } else {
+      // free stream and Dirichlet ghost states do not depend on the interior
+#pragma unroll
+      for (int v = 0; v < 4; v++) qr[v] = 0.0f;
+    }
+  }
+  Dual L[4], R[4], F[4], wsm;
+#pragma unroll
+  for (int v = 0; v < 4; v++) {
+    L[v] = Dual(pl[v], ql[v]);
+    R[v] = Dual(pr[v], qr[v]);
+  }
+  roe_flux_fast_t<Dual>(Dual(TP(gamma)), Dual(TP(gm1)), Dual(TP(igm1)), L, R, Dual(n.x), Dual(n.y), F, wsm);
+  const float f[4] = {F[0].d * af, F[1].d * af, F[2].d * af, F[3].d * af};
+  st4(static_cast<float*>(d.eflux), e, f);
+}
+
+// One cell of an RK stage of the correction with the residual R0 + J dU (the
+// same stage formulas as update_item, local dt frozen at the base state);
+// writes the primitive tangent of the new dU and, at the last stage, adds
+// |dU - dU0|^2 to d2.
+template <int MODE>
+__device__ __forceinline__ void dc_update_item(const DevView& d, const DcView& c, const StageParams& sp, int ic,
+                                               double* d2) {
+  float acc[4] = {0.f, 0.f, 0.f, 0.f};
+  const int4 cf = d.cflist[ic];
+  const int sl[4] = {cf.x, cf.y, cf.z, cf.w};
+#pragma unroll
+  for (int j = 0; j < 4; j++) {
+    const int s = sl[j];
+    if (s == 0) continue;
+    float f[4];
+    ldc4<true>(static_cast<const float*>(d.eflux), (s > 0 ? s : -s) - 1, f);
+#pragma unroll
+    for (int v = 0; v < 4; v++) acc[v] += s > 0 ? f[v] : -f[v];
+  }
+  const float rv = -static_cast<const float*>(d.volT)[ic];
+  float r0[4], res[4];
+  ld4(c.R0, ic, r0);
+#pragma unroll
+  for (int v = 0; v < 4; v++) res[v] = r0[v] + acc[v] * rv;
+  const float h = float(d.dtl[ic] * sp.cst);
+  float u0[4], u[4], f[4];
+  if (sp.stage == 1) {
+    ldc4<true>(c.D, ic, u0);
+    st4(c.D0, ic, u0);
+#pragma unroll
+    for (int v = 0; v < 4; v++) f[v] = 0.f;
+  } else {
+    ldc4<true>(c.D0, ic, u0);
+    ldc4<true>(c.DF, ic, f);
+  }
+  const float coef = float(sp.coef);
+  if (MODE == MODE_SSP42) {
+#pragma unroll
+    for (int v = 0; v < 4; v++) {
+      u[v] = u0[v] + h * (coef * res[v] + f[v]);
+      f[v] = f[v] + res[v];
+    }
+  } else {
+#pragma unroll
+    for (int v = 0; v < 4; v++) {
+      f[v] = f[v] + coef * res[v];
+      u[v] = sp.last ? u0[v] + h * f[v] : u0[v] + h * res[v];
+    }
+  }
+  if (!sp.last) st4(c.DF, ic, f);
+  st4(c.D, ic, u);
+  // tangent of cvar2pvar at the base primitives p
+  float p[4];
+  ld4(static_cast<const float*>(d.Pv), ic, p);
+  const float ri = 1.0f / p[0];
+  const float du = (u[1] - p[1] * u[0]) * ri, dv = (u[2] - p[2] * u[0]) * ri;
+  const float q[4] = {u[0], du, dv,
+                      d.fgm1 * (u[3] - 0.5f * u[0] * (p[1] * p[1] + p[2] * p[2]) - p[0] * (p[1] * du + p[2] * dv))};
+  st4(c.dP, ic, q);
+  if (sp.last) {
+#pragma unroll
+    for (int v = 0; v < 4; v++) {
+      const double dd = double(u[v] - u0[v]);
+      d2[v] += dd * dd;
+    }
+  }
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(256) k_persistent_dc(const DevView d, const PersistPlan p, const DcView c) {
+  const int nb = gridDim.x;
+  const int step0 = *p.step0_dev;
+  for (int s = 0; s < p.nsteps; s++) {
+    for (int k = 0; k < p.nstages; k++) {
+      const StageParams& sp = p.sp[k];
+      for (int t = blockIdx.x; t < p.nedge_tiles; t += nb) {
+        const int2 tl = p.edge_tiles[t];
+        for (int e = tl.x + threadIdx.x; e < tl.y; e += blockDim.x) dc_flux_item(d, c, e);
+      }
+      if (!grid_sync(p.bar, p.budget)) return;
+      for (int t = blockIdx.x; t < p.ncell_tiles; t += nb) {
+        const int4 tl = p.cell_tiles[t];
+        double d2[4] = {0.0, 0.0, 0.0, 0.0};
+        for (int ic = tl.x + threadIdx.x; ic < tl.y; ic += blockDim.x) dc_update_item<MODE>(d, c, sp, ic, d2);
+        if (sp.last) {
+          double out[4];
+          block_sum4(d2, out);
+          if (threadIdx.x == 0)
+#pragma unroll
+            for (int q = 0; q < 4; q++) p.tile_partials[4 * (size_t)t + q] = out[q];
+        }
+      }
+      if (!grid_sync(p.bar, p.budget)) return;
+    }
+    // per-case RMS of the correction increments of this step (fixed order)
+    const int slot = (step0 + s) % p.norm_cap;
+    for (int cs = blockIdx.x; cs < p.ncase_active; cs += nb) {
+      if (threadIdx.x == 0) {
+        const int4 ct = p.case_tiles[cs];
+        double a[4] = {0.0, 0.0, 0.0, 0.0};
+        for (int t = ct.y; t < ct.z; t++)
+#pragma unroll
+          for (int q = 0; q < 4; q++) a[q] += p.tile_partials[4 * (size_t)t + q];
+        double* o = p.case_norms + 4 * ((size_t)ct.x * p.norm_cap + slot);
+#pragma unroll
+        for (int q = 0; q < 4; q++) o[q] = sqrt(a[q] / double(ct.w));
+      }
+    }
+  }
+}
+
+__global__ void __launch_bounds__(256) k_dc_fold(const DevView d, const DcView c, double* U64) {
+  const int ic = blockIdx.x * blockDim.x + threadIdx.x;
+  if (ic >= d.nc) return;
+  float du[4];
+  ld4(c.D, ic, du);
+  double u[4];
+  ld4(U64, ic, u);
+#pragma unroll
+  for (int v = 0; v < 4; v++) u[v] += double(du[v]);
+  st4(U64, ic, u);
+  const float z[4] = {0.f, 0.f, 0.f, 0.f};
+  st4(c.D, ic, z);
+  st4(c.dP, ic, z);
+}
+
+__global__ void __launch_bounds__(256) k_dc_base(const DevView d, const DcView c, const double* U64,
+                                                 const double* resid64, const double* ws64) {
+  const int ic = blockIdx.x * blockDim.x + threadIdx.x;
+  if (ic >= d.nc) return;
+  double u[4], r[4];
+  ld4(U64, ic, u);
+  float p[4];
+  cons2prim(d.fgm1, u, p);
+  st4(static_cast<float*>(d.Pv), ic, p);
+  ld4(resid64, ic, r);
+  const float rf[4] = {float(r[0]), float(r[1]), float(r[2]), float(r[3])};
+  st4(c.R0, ic, rf);
+  // compute_local_time, src/runge_kutta.f90:424-437, at the base state
+  d.dtl[ic] = d.cfl * d.vol[ic] / (0.5 * ws64[ic]);
+}
+
+static void dc_fold(const DevView& d, const DcView& c, double* U64, cudaStream_t s) {
+  k_dc_fold<<<grid_of(d.nc), 256, 0, s>>>(d, c, U64);
+}
+static void dc_base(const DevView& d, const DcView& c, const double* U64, const double* resid64, const double* ws64,
+                    cudaStream_t s) {
+  k_dc_base<<<grid_of(d.nc), 256, 0, s>>>(d, c, U64, resid64, ws64);
+}
+static int dc_occupancy(int block) {
+  int n = 0;
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_persistent_dc<MODE_SSP42>, block, 0) == cudaSuccess ? n
+                                                                                                               : 0;
+}
+static cudaError_t dc_persistent(const DevView& d, const PersistPlan& p, const DcView& c, int grid, int block,
+                                 cudaStream_t s) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)grid);
+  cfg.blockDim = dim3((unsigned)block);
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  if (p.sp[0].mode == MODE_SSP42) return cudaLaunchKernelEx(&cfg, k_persistent_dc<MODE_SSP42>, d, p, c);
+  return cudaLaunchKernelEx(&cfg, k_persistent_dc<MODE_RK>, d, p, c);
+}
+#endif  // FVS_MIXED
 
 }  // namespace FVS_NS
 }  // namespace fvs

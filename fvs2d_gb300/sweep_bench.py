@@ -8,7 +8,10 @@ metric).  Runs entirely on the GPU through the C-ABI; prints one JSON object.
           absolute target, 1e-10 x the first-step RMS(dU_rho) of a
           free-stream start:
             plain    one FP64 Solver per case, one after the other
-            batched  one batch, mixed until 1e-5 x target level, then FP64
+            batched  one batch, mixed until 1e-5 x target level, then the
+                     defect-correction iteration (FP64 residual once per chunk,
+                     FP32 linearised stages) to the target, confirmed by FP64
+                     steps
             learned  the same batch started from the network's prediction
           errors: max |U - U_plain| / max|U_plain| of the final states, and
           the surrogate's error before any solver step
@@ -72,10 +75,10 @@ def run(n_train=96, n_test=24, wall=(64, 192), radial=(32, 96), max_steps=200000
     out["test"] = {
         "cells_test": int(sum(m.ncells for m in meshes)),
         "plain_fp64": {"seconds": round(t_plain, 3), "steps_total": int(steps_p.sum())},
-        "batched_ladder": {"seconds": round(t_batch, 3), "steps_mixed": int(b1.max()), "steps_fp64": int(b2.max()),
+        "batched_ladder": {"seconds": round(t_batch, 3), "steps_mixed": int(b1.max()), "steps_after_switch": int(b2.max()),
                            "linf_vs_plain": err(st_b, plain_states),
                            "phase_seconds": {k: round(v, 3) for k, v in ph_b.items()}},
-        "learned_batched_ladder": {"seconds": round(t_learn, 3), "steps_mixed": int(l1.max()), "steps_fp64": int(l2.max()),
+        "learned_batched_ladder": {"seconds": round(t_learn, 3), "steps_mixed": int(l1.max()), "steps_after_switch": int(l2.max()),
                                    "linf_vs_plain": err(st_l, plain_states),
                                    "phase_seconds": {k: round(v, 3) for k, v in ph_l.items()}},
         "speedup_batched_vs_plain": round(t_plain / t_batch, 2),

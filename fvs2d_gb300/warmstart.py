@@ -49,10 +49,12 @@ def targets(case: sweep.Case, cvar: np.ndarray) -> np.ndarray:
 
 
 def solve_ladder(meshes, opts_mixed, levels, switch=1e-5, drop=1e-10, max_steps=200000, chunk=200, starts=None,
-                 autotune=True):
+                 autotune=True, dc=True):
     """Batched precision-ladder solve to levels*drop (levels: per-case
-    reference residuals [ncases][4]).  Returns (states, steps_mixed,
-    steps_fp64, seconds, phase seconds {setup, tune, mixed, fp64})."""
+    reference residuals [ncases][4]): mixed precision to levels*switch, then
+    (dc) the defect-correction iteration to levels*drop followed by the FP64
+    iteration, which confirms the levels, or (not dc) FP64 alone.  Returns
+    (states, steps_mixed, steps after the switch, seconds, phase seconds)."""
     t0 = time.perf_counter()
     phases = {}
     with Batch(meshes, opts_mixed) as b:
@@ -69,8 +71,15 @@ def solve_ladder(meshes, opts_mixed, levels, switch=1e-5, drop=1e-10, max_steps=
         n1, _, _, _ = b.run_to_level(max_steps, np.asarray(levels) * switch, chunk)
         t3 = time.perf_counter()
         phases["mixed"] = t3 - t2
+        n2 = np.zeros_like(n1)
+        if dc:
+            n2, _, _, _ = b.run_to_level(max_steps, np.asarray(levels) * drop, chunk, dc=True)
+            t4 = time.perf_counter()
+            phases["dc"] = t4 - t3
+            t3 = t4
         b.set_precision(PREC_FP64)
-        n2, _, last, _ = b.run_to_level(max_steps, np.asarray(levels) * drop, chunk)
+        n3, _, last, _ = b.run_to_level(max_steps, np.asarray(levels) * drop, 10 if dc else chunk)
+        n2 = n2 + n3
         phases["fp64"] = time.perf_counter() - t3
         states = [b.get_state(c) for c in range(b.ncases)]
     return states, n1, n2, time.perf_counter() - t0, phases

@@ -258,6 +258,16 @@ int fvs_batch_run_to_drop(fvs_batch* b, int32_t max_steps, double drop, int32_t 
  * (a warm start judged on the thresholds of a free-stream start) */
 int fvs_batch_run_to_level(fvs_batch* b, int32_t max_steps, const double* levels, int32_t chunk, int32_t* steps_done,
                            double* first, double* last, float* ms);
+/* Defect correction for first-order steady batches (no counterpart in the
+ * reference): per chunk of `chunk` steps the FP64 residual R0 of the current
+ * state is evaluated once, then the RK stages iterate a correction dU with
+ * the linearised residual R0 + J dU (J dU by forward-mode differentiation of
+ * the Roe flux in FP32) and the correction is added to the FP64 state.  The
+ * fixed point is the FP64 residual's.  Norms are the RMS of the correction
+ * increments per step; stops like fvs_batch_run_to_level.  The batch is in
+ * FP64 afterwards (confirm the levels with fvs_batch_run_to_level). */
+int fvs_batch_run_to_level_dc(fvs_batch* b, int32_t max_steps, const double* levels, int32_t chunk,
+                              int32_t* steps_done, double* first, double* last, float* ms);
 
 /* ---- learned warm start: a small MLP on the GPU ---------------------------
  * No counterpart in the reference.  n_in -> width (GELU) x depth -> n_out,

@@ -1,0 +1,73 @@
+"""Defect-correction iteration of first-order steady batches.
+
+Each chunk evaluates the FP64 residual R0 of the current state once and then
+iterates a correction with R0 + J dU, J dU from the FP32 dual-number Roe
+flux.  With one step per chunk, a DC step differs from an FP64 RK step only
+by the second-order remainder of the linearisation and FP32 rounding of
+J dU, so the two trajectories agree to a small fraction of the increments;
+a wrong Jacobian term would show at the size of the increments themselves.
+Converged, the state is a fixed point of the FP64 iteration.
+"""
+import numpy as np
+import pytest
+
+import cases
+from fvs2d_gb300 import PREC_FP64, PREC_MIXED, Solver
+from fvs2d_gb300.batch import Batch
+
+pytestmark = pytest.mark.gpu
+
+
+def first_order_sweep(prec=PREC_MIXED):
+    specs = [(48, 16, 0.5, 0.0), (64, 20, 0.7, 1.5), (40, 24, 0.3, -2.0)]
+    meshes, opts = [], []
+    for nw, nr, mach, aoa in specs:
+        m, o = cases.airfoil(nw=nw, nr=nr, mach_inf=mach, aoa_inf_deg=aoa, reconst=1, limiter=0, precision=prec)
+        meshes.append(m)
+        opts.append(o)
+    return meshes, opts
+
+
+def test_one_step_chunks_follow_the_fp64_trajectory():
+    meshes, opts = first_order_sweep(PREC_FP64)
+    with Batch(meshes, opts) as b:
+        b.initialize_solution()
+        b.steps(300)
+        start = [b.get_state(c) for c in range(3)]
+        b.steps(6)
+        ref = [b.get_state(c) for c in range(3)]
+        for c in range(3):
+            b.set_state(c, start[c])
+        never = np.zeros((3, 4))  # levels no case reaches: exactly max_steps steps
+        done, first, last, _ = b.run_to_level(6, never, chunk=1, dc=True)
+        assert np.all(done == 6)
+        got = [b.get_state(c) for c in range(3)]
+    for c in range(3):
+        inc = np.abs(ref[c] - start[c]).max()
+        err = np.abs(got[c] - ref[c]).max()
+        assert inc > 0
+        assert err <= 1e-3 * inc, (c, err, inc)
+
+
+def test_converges_to_the_fp64_fixed_point():
+    meshes, opts = first_order_sweep(PREC_MIXED)
+    with Batch(meshes, opts) as b:
+        b.initialize_solution()
+        first, _ = b.steps(1)
+        levels = first[:, 0, :] * 1e-9
+        b.initialize_solution()
+        n1, _, _, _ = b.run_to_level(100000, levels * 1e4, chunk=200)
+        n2, _, last, _ = b.run_to_level(100000, levels, chunk=200, dc=True)
+        assert np.all(n2 < 100000)
+        assert np.all(last <= levels)
+        # the FP64 iteration from the corrected state meets the levels at once
+        n3, f3, _, _ = b.run_to_level(1000, levels * 1.5, chunk=10)
+        assert np.all(n3 <= 10), n3
+        states = [b.get_state(c) for c in range(3)]
+    for c in range(3):
+        with Solver(meshes[c], opts[c].replace(precision=PREC_FP64)) as s:
+            s.initialize_solution()
+            r0, _ = s.compute_residual(0.0)
+            s.cvar = states[c]
+            r, _ = s.compute_residual(0.0)
+        assert np.abs(r).max() <= 1e-7 * np.abs(r0).max(), (c, np.abs(r).max(), np.abs(r0).max())
