@@ -164,11 +164,12 @@ def run_ours(args) -> dict:
     import torch
     import torch.distributed as tdist
 
-    from fvs2d_gb300 import PREC_FP64, PREC_FP64_STRICT, PREC_MIXED, Solver, _build
+    from fvs2d_gb300 import PREC_FP64, PREC_FP64_DF, PREC_FP64_STRICT, PREC_MIXED, Solver, _build
     _build.build()
     if ws > 1:
         tdist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
-    prec = {"fp64": PREC_FP64, "fp64_strict": PREC_FP64_STRICT, "mixed": PREC_MIXED}[args.precision]
+    prec = {"fp64": PREC_FP64, "fp64_strict": PREC_FP64_STRICT, "mixed": PREC_MIXED,
+            "fp64_df": PREC_FP64_DF}[args.precision]
     mesh, opt = workload(prec)
     s = Solver(mesh, opt)
     s.initialize_solution()
@@ -242,8 +243,9 @@ def run_ours(args) -> dict:
 
     if rank == 0 and args.variants:
         var = {}
-        for name, pr, gm in (("mixed_lsq", PREC_MIXED, 3), ("fp64_strict_lsq", PREC_FP64_STRICT, 3),
-                             ("fp64_ggcb", PREC_FP64, 1), ("fp64_ggnb", PREC_FP64, 2), ("mixed_ggnb", PREC_MIXED, 2)):
+        for name, pr, gm in (("mixed_lsq", PREC_MIXED, 3), ("fp64_df_lsq", PREC_FP64_DF, 3),
+                             ("fp64_strict_lsq", PREC_FP64_STRICT, 3), ("fp64_ggcb", PREC_FP64, 1),
+                             ("fp64_ggnb", PREC_FP64, 2), ("mixed_ggnb", PREC_MIXED, 2), ("fp64_df_ggnb", PREC_FP64_DF, 2)):
             m2, o2 = workload(pr, gm)
             with Solver(m2, o2) as s2:
                 s2.initialize_solution()
@@ -345,20 +347,22 @@ def main():
     ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "fp64_strict", "mixed"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "fp64_strict", "mixed", "fp64_df"])
     ap.add_argument("--no-variants", dest="variants", action="store_false")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=12.0)
-    ap.add_argument("--workload", default="vortex", choices=["vortex", "sweep"],
+    ap.add_argument("--workload", default="vortex", choices=["vortex", "sweep", "airfoil"],
                     help="vortex: the 1,048,576-cell throughput case (default); sweep: time to a 1e-10 drop on an "
-                         "airfoil sweep, plain FP64 vs batched ladder vs learned warm start")
+                         "airfoil sweep, plain FP64 vs batched ladder vs learned warm start; airfoil: time to a "
+                         "1e-10 drop on the 261,120-cell NACA0012 O-grid, plain FP64 vs the ladder")
     ap.add_argument("--n-train", type=int, default=96)
     ap.add_argument("--n-test", type=int, default=24)
     args = ap.parse_args()
-    if args.workload == "sweep":
+    if args.workload in ("sweep", "airfoil"):
         from fvs2d_gb300 import _build, sweep_bench
         _build.build()
-        print(json.dumps(sweep_bench.run(args.n_train, args.n_test)), flush=True)
+        out = sweep_bench.run(args.n_train, args.n_test) if args.workload == "sweep" else sweep_bench.run_airfoil()
+        print(json.dumps(out), flush=True)
         return
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3

@@ -7,10 +7,10 @@ options (:mod:`.options`) and the synthetic meshes of the benchmark cases
 (:mod:`.meshgen`).  There is no CPU fallback: a missing library raises.
 """
 from . import capi, meshgen
-from .capi import PREC_FP64, PREC_FP64_STRICT, PREC_MIXED
+from .capi import PREC_FP64, PREC_FP64_DF, PREC_FP64_STRICT, PREC_MIXED
 from .meshgen import Mesh
 from .options import Options, read_input
 from .solver import FvsError, Solver
 
-__all__ = ["capi", "meshgen", "Mesh", "Options", "read_input", "Solver", "FvsError", "PREC_FP64", "PREC_FP64_STRICT",
+__all__ = ["capi", "meshgen", "Mesh", "Options", "read_input", "Solver", "FvsError", "PREC_FP64", "PREC_FP64_DF", "PREC_FP64_STRICT",
            "PREC_MIXED"]

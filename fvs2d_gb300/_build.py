@@ -28,11 +28,12 @@ UNITS = {
     "fvs_kern_strict.cu": ["-fmad=false"],
     "fvs_kern_fast.cu": ["-fmad=true"],
     "fvs_kern_mixed.cu": ["-fmad=true"],
+    "fvs_kern_df.cu": ["-fmad=true"],
     "fvs_noalloc.cu": [],
     "fvs_batch.cu": [],
     "fvs_mlp.cu": [],
 }
-HEADERS = ["fvs_internal.hpp", "fvs_kernels.cuh", "fvs_layout.hpp"]
+HEADERS = ["fvs_internal.hpp", "fvs_kernels.cuh", "fvs_layout.hpp", "df64.cuh"]
 
 
 def nvcc() -> str:

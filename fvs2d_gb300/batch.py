@@ -102,6 +102,17 @@ class Batch:
                                                     capi.ptr(first), capi.ptr(last), C.byref(ms)))
         return done, first, last, ms.value
 
+    def set_groups(self, group=None) -> None:
+        """Cases with the same group id stop together when the first of them
+        meets its target (None: every case alone)."""
+        if group is None:
+            self._check(self._lib.fvs_batch_set_groups(self._h, None))
+            return
+        g = np.ascontiguousarray(group, np.int32)
+        if g.shape != (self.ncases,):
+            raise ValueError("one group id per case")
+        self._check(self._lib.fvs_batch_set_groups(self._h, capi.ptr(g)))
+
     def run_to_level(self, max_steps: int, levels, chunk: int = 50, dc: bool = False):
         """Steps until each case's RMS(dU_k) <= levels[c, k] for all k; same
         returns as run_to_drop.  dc: defect-correction iteration (first-order

@@ -25,6 +25,7 @@ ERROR_NAMES = {0: "FVS_OK", 1: "FVS_ERR_INVALID", 2: "FVS_ERR_MESH", 3: "FVS_ERR
 PREC_FP64_STRICT = 0
 PREC_FP64 = 1
 PREC_MIXED = 2
+PREC_FP64_DF = 3
 
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int32)
@@ -100,6 +101,7 @@ SIGNATURES = {
     "fvs_batch_steps": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.POINTER(C.c_float)]),
     "fvs_batch_run_to_drop": (C.c_int, [C.c_void_p, C.c_int32, C.c_double, C.c_int32, C.c_void_p, C.c_void_p,
                                         C.c_void_p, C.POINTER(C.c_float)]),
+    "fvs_batch_set_groups": (C.c_int, [C.c_void_p, C.c_void_p]),
     "fvs_batch_run_to_level": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p,
                                          C.c_void_p, C.POINTER(C.c_float)]),
     "fvs_batch_run_to_level_dc": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p,

@@ -22,6 +22,7 @@
 #include <thread>
 #include <vector>
 
+#include "df64.cuh"
 #include "fvs_internal.hpp"
 #include "fvs_layout.hpp"
 
@@ -76,7 +77,7 @@ struct fvs_batch {
     bool built = false;
     DevView d;
     int block = 256, tile = 1024, bps = 1;
-  } var[3];
+  } var[4];
   int nc = 0, ne = 0;
   std::vector<int> coff, eoff, cnum, enumv;  // per-case cell / edge-slot ranges
   std::vector<double> pinf;                 // [ncases][4]
@@ -105,6 +106,7 @@ struct fvs_batch {
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   int* h_step0 = nullptr;
   DcView dc;  // defect-correction arrays, allocated on first use
+  std::vector<int> group;  // cases of one group stop together (first to converge)
 
   ~fvs_batch() {
     if (graph) cudaGraphExecDestroy(graph);
@@ -161,6 +163,12 @@ int build_batch_device(fvs_batch* B, DevView& d) {
   return FVS_OK;
 }
 
+int build_for(fvs_batch* B, int prec, DevView& d) {
+  if (prec == FVS_PREC_MIXED) return build_batch_device<float>(B, d);
+  if (prec == FVS_PREC_FP64_DF) return build_batch_device<df64>(B, d);
+  return build_batch_device<double>(B, d);
+}
+
 int alloc_batch_buffers(fvs_batch* B) {
   void* p;
   bool ok = B->arena.alloc(p, 32 * (size_t)B->nc);
@@ -182,8 +190,7 @@ void init_view_constants(fvs_batch* B, DevView& d) {
   const fvs_options& ob = B->base;
   d.gamma = ob.gamma; d.gm1 = ob.gamma - 1.0; d.igm1 = 1.0 / (ob.gamma - 1.0);
   d.khalf = ob.umuscl / 2.0; d.nkhalf = -ob.umuscl / 2.0; d.omk = 1.0 - ob.umuscl; d.cfl = ob.cfl;
-  d.fgamma = float(d.gamma); d.fgm1 = float(d.gm1); d.figm1 = float(d.igm1);
-  d.fkhalf = float(d.khalf); d.fnkhalf = float(d.nkhalf); d.fomk = float(d.omk);
+  set_fp32_constants(d);
   d.limiter = ob.limiter; d.grad_method = ob.grad_method; d.first_order = ob.reconst == FVS_RECON_UPWIND1;
   d.vortex = ob.vortex; d.vx = ob.vortex_x; d.vy = ob.vortex_y; d.vkappa = ob.vortex_kappa;
   for (int k = 0; k < 4; k++) { d.vinf[k] = ob.vortex_inf[k]; d.pinf[k] = B->pinf[k]; }
@@ -192,8 +199,10 @@ void init_view_constants(fvs_batch* B, DevView& d) {
 }
 
 const KernelSet* kernels_for(int prec) {
-  return prec == FVS_PREC_MIXED ? &kernels_mixed()
-         : (prec == FVS_PREC_FP64_STRICT ? &kernels_fp64_strict() : &kernels_fp64_fast());
+  return prec == FVS_PREC_MIXED         ? &kernels_mixed()
+         : prec == FVS_PREC_FP64_STRICT ? &kernels_fp64_strict()
+         : prec == FVS_PREC_FP64_DF     ? &kernels_fp64_df()
+                                        : &kernels_fp64_fast();
 }
 
 void set_batch_stages(fvs_batch* B) {
@@ -344,7 +353,7 @@ int variant_view(fvs_batch* B, int prec, DevView** out) {
     init_view_constants(B, v.d);
     const int cur = B->prec;  // build_batch_device reads the precision
     B->prec = prec;
-    int rc = prec == FVS_PREC_MIXED ? build_batch_device<float>(B, v.d) : build_batch_device<double>(B, v.d);
+    int rc = build_for(B, prec, v.d);
     B->prec = cur;
     if (rc) return rc;
     v.built = true;
@@ -430,7 +439,7 @@ int fvs_batch_create(const fvs_mesh* meshes, const fvs_options* opts, int32_t nc
   cudaEventCreate(&B->ev1);
   cudaDeviceGetAttribute(&B->nsm, cudaDevAttrMultiProcessorCount, 0);
   init_view_constants(B.get(), B->d);
-  int rc = B->mixed ? build_batch_device<float>(B.get(), B->d) : build_batch_device<double>(B.get(), B->d);
+  int rc = build_for(B.get(), B->prec, B->d);
   if (!rc) rc = alloc_batch_buffers(B.get());
   if (rc) { g_batch_create_error = B->err; return rc; }
   set_batch_stages(B.get());
@@ -504,7 +513,7 @@ int fvs_batch_init_state(fvs_batch* b) {
 // phase followed by an FP64 phase).  The other precision's device layout is
 // built on first use from the stored host meshes; the FP64 state is copied.
 int fvs_batch_set_precision(fvs_batch* b, int32_t precision) {
-  if (!b || precision < 0 || precision > 2) return FVS_ERR_INVALID;
+  if (!b || precision < 0 || precision > 3) return FVS_ERR_INVALID;
   if (precision == b->prec) return FVS_OK;
   fvs_batch::Variant& cur = b->var[b->prec];
   cur.built = true;
@@ -515,7 +524,7 @@ int fvs_batch_set_precision(fvs_batch* b, int32_t precision) {
   b->prec = precision;
   if (!nxt.built) {
     init_view_constants(b, nxt.d);
-    int rc = precision == FVS_PREC_MIXED ? build_batch_device<float>(b, nxt.d) : build_batch_device<double>(b, nxt.d);
+    int rc = build_for(b, precision, nxt.d);
     if (rc) {
       b->prec = old_prec;
       return rc;
@@ -535,6 +544,16 @@ int fvs_batch_set_precision(fvs_batch* b, int32_t precision) {
   b->plan_dirty = true;
   e = cudaStreamSynchronize(b->stream);
   return e == cudaSuccess ? FVS_OK : b->cuda_fail(e, "precision switch");
+}
+
+int fvs_batch_set_groups(fvs_batch* b, const int32_t* group) {
+  if (!b) return FVS_ERR_INVALID;
+  if (!group) {
+    b->group.clear();
+    return FVS_OK;
+  }
+  b->group.assign(group, group + b->ncases);
+  return FVS_OK;
 }
 
 int fvs_batch_set_barrier_budget(fvs_batch* b, double seconds) {
@@ -617,6 +636,17 @@ int fvs_batch_autotune(fvs_batch* b, int32_t trial_steps, float* best_ms) {
   return FVS_OK;
 }
 
+// A case that converged ends the other cases of its group at the same step
+// (several starts of one problem raced against each other).
+void stop_group(fvs_batch* b, int c, int at, std::vector<int>& done) {
+  if (b->group.empty()) return;
+  for (int k = 0; k < b->ncases; k++)
+    if (k != c && b->active[k] && b->group[k] == b->group[c]) {
+      b->active[k] = 0;
+      done[k] = at;
+    }
+}
+
 // Steps all cases until each one's RMS(dU_rho) falls to drop x its first
 // value (or max_steps).  steps_done[c] = the step at which case c reached the
 // drop (max_steps if it did not); first/last [ncases][4] norms.
@@ -629,6 +659,7 @@ static int run_until(fvs_batch* b, int32_t max_steps, double drop, const double*
   std::fill(b->active.begin(), b->active.end(), 1);
   b->plan_dirty = true;
   std::vector<double> all(4 * (size_t)nc * b->norm_cap);
+  std::vector<int> conv_now;
   cudaEventRecord(b->ev0, b->stream);
   int step = 0, rc = FVS_OK;
   bool nonfinite = false;
@@ -655,11 +686,16 @@ static int run_until(fvs_batch* b, int32_t max_steps, double drop, const double*
           done[c] = step + s + 1;
           b->active[c] = 0;
           changed = true;
+          conv_now.push_back(c);
           break;
         }
       }
-      nact += b->active[c];
     }
+    // the earliest converged case of a group ends the group
+    std::sort(conv_now.begin(), conv_now.end(), [&](int x, int y) { return done[x] < done[y]; });
+    for (int c : conv_now) stop_group(b, c, done[c], done);
+    conv_now.clear();
+    for (int c = 0; c < nc; c++) nact += b->active[c];
     step += n;
     if (nact == 0) break;
     if (changed) b->plan_dirty = true;
@@ -719,6 +755,7 @@ int fvs_batch_run_to_level_dc(fvs_batch* b, int32_t max_steps, const double* lev
   std::fill(b->active.begin(), b->active.end(), 1);
   b->plan_dirty = true;
   std::vector<double> all(4 * (size_t)nc * b->norm_cap);
+  std::vector<int> conv_now;
   cudaEventRecord(b->ev0, b->stream);
   int step = 0;
   bool nonfinite = false;
@@ -755,11 +792,16 @@ int fvs_batch_run_to_level_dc(fvs_batch* b, int32_t max_steps, const double* lev
           done[c] = step + s + 1;
           b->active[c] = 0;
           changed = true;
+          conv_now.push_back(c);
           break;
         }
       }
-      nact += b->active[c];
     }
+    // the earliest converged case of a group ends the group
+    std::sort(conv_now.begin(), conv_now.end(), [&](int x, int y) { return done[x] < done[y]; });
+    for (int c : conv_now) stop_group(b, c, done[c], done);
+    conv_now.clear();
+    for (int c = 0; c < nc; c++) nact += b->active[c];
     step += n;
     if (nact == 0) break;
     if (changed) b->plan_dirty = true;

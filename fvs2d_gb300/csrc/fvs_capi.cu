@@ -15,6 +15,7 @@
 #include <string>
 #include <vector>
 
+#include "df64.cuh"
 #include "fvs_internal.hpp"
 #include "fvs_layout.hpp"
 
@@ -106,6 +107,7 @@ struct fvs_handle {
   std::string err;
   const KernelSet* ks = nullptr;
   bool mixed = false;
+  bool df = false;  // double-float kernels (FVS_PREC_FP64_DF)
   cudaStream_t stream = nullptr;
   DeviceArena arena;
   DevView d;
@@ -306,7 +308,7 @@ int validate_options(const fvs_options* o, std::string& err) {
   const int ns = o->rk_nstages;
   bool ok = (ns == 4 && o->rk_order >= 1 && o->rk_order <= 4 && (!o->ssprk || o->rk_order == 2)) || (ns == 3 && o->ssprk);
   if (!ok) { err = "RK coefficients exist for 4 stages (SSP: order 2) and the SSP-RK3 extension only"; return FVS_ERR_INVALID; }
-  if (o->precision < 0 || o->precision > 2) { err = "precision must be 0, 1 or 2"; return FVS_ERR_INVALID; }
+  if (o->precision < 0 || o->precision > 3) { err = "precision must be 0, 1, 2 or 3"; return FVS_ERR_INVALID; }
   if (!(o->gamma > 1.0)) { err = "gamma must be > 1"; return FVS_ERR_INVALID; }
   return FVS_OK;
 }
@@ -357,8 +359,9 @@ int fvs_create(const fvs_mesh* mesh, const fvs_options* opt, fvs_handle** out) {
   H->pvar_inf[2] = H->o.mach_inf * std::sin(aoa);
   H->pvar_inf[3] = 1.0 / H->o.gamma;
   H->mixed = H->o.precision == FVS_PREC_MIXED;
+  H->df = H->o.precision == FVS_PREC_FP64_DF;
   H->ks = H->o.precision == FVS_PREC_FP64_STRICT ? &kernels_fp64_strict()
-          : H->mixed ? &kernels_mixed() : &kernels_fp64_fast();
+          : H->mixed ? &kernels_mixed() : H->df ? &kernels_fp64_df() : &kernels_fp64_fast();
   cudaError_t e = cudaStreamCreateWithFlags(&H->stream, cudaStreamNonBlocking);
   if (e != cudaSuccess) { g_create_error = std::string("cudaStreamCreate: ") + cudaGetErrorString(e); return FVS_ERR_CUDA; }
   if (cudaMallocHost(&H->h_small, 64) != cudaSuccess) { g_create_error = "pinned allocation failed"; return FVS_ERR_NOMEM; }
@@ -372,8 +375,7 @@ int fvs_create(const fvs_mesh* mesh, const fvs_options* opt, fvs_handle** out) {
   d.cfl = H->o.cfl;
   d.gm1 = H->o.gamma - 1.0;
   d.igm1 = 1.0 / (H->o.gamma - 1.0);
-  d.fgamma = float(d.gamma); d.fgm1 = float(d.gm1); d.figm1 = float(d.igm1);
-  d.fkhalf = float(d.khalf); d.fnkhalf = float(d.nkhalf); d.fomk = float(d.omk);
+  set_fp32_constants(d);
   d.limiter = H->o.limiter;
   d.grad_method = H->o.grad_method;
   d.first_order = H->o.reconst == FVS_RECON_UPWIND1;
@@ -381,7 +383,7 @@ int fvs_create(const fvs_mesh* mesh, const fvs_options* opt, fvs_handle** out) {
   d.vx = H->o.vortex_x; d.vy = H->o.vortex_y; d.vkappa = H->o.vortex_kappa;
   for (int k = 0; k < 4; k++) { d.vinf[k] = H->o.vortex_inf[k]; d.pinf[k] = H->pvar_inf[k]; }
   mms_constants(d.mc);
-  rc = H->mixed ? build_device<float>(H.get()) : build_device<double>(H.get());
+  rc = H->mixed ? build_device<float>(H.get()) : H->df ? build_device<df64>(H.get()) : build_device<double>(H.get());
   if (rc) { g_create_error = H->err; return rc; }
   H->dt = H->o.dt;
   // steady runs start from dt_local = dt (src/runge_kutta.f90:73-76)
@@ -511,12 +513,18 @@ int fvs_get_gradient(fvs_handle* h, double* grad, double* phi) {
     if (h->mixed) {
       if ((rc = typed_out<float>(h, h->d.Gx, grad, 4))) return rc;
       if ((rc = typed_out<float>(h, h->d.Gy, grad + 4 * (size_t)nc, 4))) return rc;
+    } else if (h->df) {
+      if ((rc = typed_out<df64>(h, h->d.Gx, grad, 4))) return rc;
+      if ((rc = typed_out<df64>(h, h->d.Gy, grad + 4 * (size_t)nc, 4))) return rc;
     } else {
       if ((rc = typed_out<double>(h, h->d.Gx, grad, 4))) return rc;
       if ((rc = typed_out<double>(h, h->d.Gy, grad + 4 * (size_t)nc, 4))) return rc;
     }
   }
-  if (phi) rc = h->mixed ? typed_out<float>(h, h->d.phi, phi, 1) : typed_out<double>(h, h->d.phi, phi, 1);
+  if (phi)
+    rc = h->mixed ? typed_out<float>(h, h->d.phi, phi, 1)
+         : h->df  ? typed_out<df64>(h, h->d.phi, phi, 1)
+                  : typed_out<double>(h, h->d.phi, phi, 1);
   return rc;
 }
 
@@ -656,6 +664,7 @@ int fvs_wall_loads(fvs_handle* h, int32_t ib, double* edge_out, double* loads) {
   const int g0 = h->d.nint + m.b_eptr[ib - 1];
   double* sums = h->d_wall + 4 * (size_t)n;
   if (h->mixed) k_wall_loads<float><<<1, 256, 0, h->stream>>>(h->d, g0, n, c2, h->pvar_inf[3], h->d_wall, sums);
+  else if (h->df) k_wall_loads<df64><<<1, 256, 0, h->stream>>>(h->d, g0, n, c2, h->pvar_inf[3], h->d_wall, sums);
   else k_wall_loads<double><<<1, 256, 0, h->stream>>>(h->d, g0, n, c2, h->pvar_inf[3], h->d_wall, sums);
   int rc = check_launch(h, "wall-load kernels");
   if (rc) return rc;

@@ -124,12 +124,27 @@ struct DevView {
   double gm1 = 0.4, igm1 = 2.5;  // gamma-1 and 1/(gamma-1)
   // the same constants rounded once on the host for the FP32 kernels
   float fgamma = 1.4f, fgm1 = 0.4f, figm1 = 2.5f, fkhalf = 0, fnkhalf = 0, fomk = 1;
+  // and split into FP32 pairs (hi, lo) for the double-float kernels
+  float dgamma[2] = {1.4f, 0}, dgm1[2] = {0.4f, 0}, digm1[2] = {2.5f, 0}, dkhalf[2] = {0, 0}, dnkhalf[2] = {0, 0},
+        domk[2] = {1, 0};
   const void* volT = nullptr;    // [nc] 1/vol in the compute type (GG gradients)
   int limiter = 0, grad_method = 3, first_order = 0, vortex = 0;
   double vx = 0, vy = 0, vkappa = 0, vinf[4] = {0, 0, 0, 0};
   double pinf[4] = {0, 0, 0, 0};
   double mc[16];
 };
+
+// FP32 constants of the scheme: rounded, and split into (hi, lo) pairs
+inline void set_fp32_constants(DevView& d) {
+  auto split = [](double x, float* o) {
+    o[0] = float(x);
+    o[1] = float(x - double(o[0]));
+  };
+  d.fgamma = float(d.gamma); d.fgm1 = float(d.gm1); d.figm1 = float(d.igm1);
+  d.fkhalf = float(d.khalf); d.fnkhalf = float(d.nkhalf); d.fomk = float(d.omk);
+  split(d.gamma, d.dgamma); split(d.gm1, d.dgm1); split(d.igm1, d.digm1);
+  split(d.khalf, d.dkhalf); split(d.nkhalf, d.dnkhalf); split(d.omk, d.domk);
+}
 
 struct StageParams {
   int stage = 1, nstages = 4, mode = MODE_RK, steady = 0, last = 0;
@@ -217,5 +232,6 @@ const DcKernels& dc_kernels();
 const KernelSet& kernels_fp64_strict();
 const KernelSet& kernels_fp64_fast();
 const KernelSet& kernels_mixed();
+const KernelSet& kernels_fp64_df();
 
 }  // namespace fvs

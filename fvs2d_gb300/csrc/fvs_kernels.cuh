@@ -6,6 +6,9 @@
 //   fvs_kern_fast.cu    FP64, -fmad=true (FMA contraction allowed)
 //   fvs_kern_mixed.cu   T = float for gradient, limiter, reconstruction and
 //                       flux; FP64 residual accumulation, update and norms
+//   fvs_kern_df.cu      T = df64 (FP64 accuracy from FP32 pairs, df64.cuh)
+//                       for gradient, limiter, reconstruction, flux and the
+//                       slot gather; FP64 state update and norms
 // FVS_NS names the namespace, FVS_T the compute type.
 //
 // One RK stage is three launches, all coalesced one-thread-per-item gathers:
@@ -24,7 +27,12 @@
 
 #include <cuda_runtime.h>
 
+#include "df64.cuh"
 #include "fvs_internal.hpp"
+
+#ifndef FVS_DF
+#define FVS_DF 0
+#endif
 
 namespace fvs {
 namespace FVS_NS {
@@ -49,6 +57,16 @@ __device__ __forceinline__ void ld4(const float* __restrict__ p, int i, float* o
 __device__ __forceinline__ void st4(float* __restrict__ p, int i, const float* v) {
   reinterpret_cast<float4*>(p)[i] = make_float4(v[0], v[1], v[2], v[3]);
 }
+__device__ __forceinline__ void ld4(const df64* __restrict__ p, int i, df64* o) {
+  const float4* q = reinterpret_cast<const float4*>(p) + 2 * (size_t)i;
+  const float4 a = q[0], b = q[1];
+  o[0] = df64(a.x, a.y); o[1] = df64(a.z, a.w); o[2] = df64(b.x, b.y); o[3] = df64(b.z, b.w);
+}
+__device__ __forceinline__ void st4(df64* __restrict__ p, int i, const df64* v) {
+  float4* q = reinterpret_cast<float4*>(p) + 2 * (size_t)i;
+  q[0] = make_float4(v[0].hi, v[0].lo, v[1].hi, v[1].lo);
+  q[1] = make_float4(v[2].hi, v[2].lo, v[3].hi, v[3].lo);
+}
 __device__ __forceinline__ T2 ld2(const void* p, int i) {
   return reinterpret_cast<const T2*>(p)[i];
 }
@@ -70,14 +88,29 @@ __device__ __forceinline__ void ldc4(const float* p, int i, float* o) {
   const float4 a = COH ? __ldcg(q) : *q;
   o[0] = a.x; o[1] = a.y; o[2] = a.z; o[3] = a.w;
 }
+template <bool COH>
+__device__ __forceinline__ void ldc4(const df64* p, int i, df64* o) {
+  const float4* q = reinterpret_cast<const float4*>(p) + 2 * (size_t)i;
+  float4 a, b;
+  if (COH) { a = __ldcg(q); b = __ldcg(q + 1); }
+  else { a = q[0]; b = q[1]; }
+  o[0] = df64(a.x, a.y); o[1] = df64(a.z, a.w); o[2] = df64(b.x, b.y); o[3] = df64(b.z, b.w);
+}
 template <bool COH, typename V>
 __device__ __forceinline__ V ldc1(const V* p, int i) {
   return COH ? __ldcg(p + i) : p[i];
+}
+template <bool COH>
+__device__ __forceinline__ df64 ldc1(const df64* p, int i) {
+  const float2 a = COH ? __ldcg(reinterpret_cast<const float2*>(p) + i) : reinterpret_cast<const float2*>(p)[i];
+  return df64(a.x, a.y);
 }
 
 // scheme constants in the compute type, rounded once on the host
 #if FVS_MIXED
 #define TP(name) (d.f##name)
+#elif FVS_DF
+#define TP(name) (df64(d.d##name[0], d.d##name[1]))
 #else
 #define TP(name) (d.name)
 #endif
@@ -380,6 +413,19 @@ __device__ __forceinline__ double tsin_(double x) { return sin(x); }
 __device__ __forceinline__ float tsin_(float x) { return sinf(x); }
 __device__ __forceinline__ double tcos_(double x) { return cos(x); }
 __device__ __forceinline__ float tcos_(float x) { return cosf(x); }
+// double-float: boundary values of the Dirichlet states, evaluated in FP64
+__device__ __forceinline__ df64 texp_(df64 x) { return df_from_double(exp(double(x))); }
+__device__ __forceinline__ df64 tpow_(df64 x, df64 y) { return df_from_double(pow(double(x), double(y))); }
+__device__ __forceinline__ df64 tsin_(df64 x) { return df_from_double(sin(double(x))); }
+__device__ __forceinline__ df64 tcos_(df64 x) { return df_from_double(cos(double(x))); }
+// an FP64 value in the compute type
+__device__ __forceinline__ T to_t(double x) {
+#if FVS_DF
+  return df_from_double(x);
+#else
+  return T(x);
+#endif
+}
 
 __device__ __forceinline__ void ghost_state(const DevView& d, int rec, double time, T x, T y, T nx, T ny,
                                             const T* pfL, T* pfR) {
@@ -388,7 +434,7 @@ __device__ __forceinline__ void ghost_state(const DevView& d, int rec, double ti
     // the free stream of the slot's case (batched meshes), else the handle's
     const double* pi = d.case_pinf ? d.case_pinf + 4 * (rec >> 4) : d.pinf;
 #pragma unroll
-    for (int k = 0; k < 4; k++) pfR[k] = T(pi[k]);
+    for (int k = 0; k < 4; k++) pfR[k] = to_t(pi[k]);
   } else if (type == FVS_BC_SLIP_WALL) {
     const T un = pfL[1] * nx + pfL[2] * ny;
     pfR[0] = pfL[0];
@@ -523,6 +569,33 @@ __device__ __forceinline__ void cell_residual(const DevView& d, int ic, double* 
   for (int v = 0; v < 4; v++) res[v] = (f2d_bits(hi[v]) + f2d_bits(lo[v])) * rv;
   ws = WS ? f2d_bits(wh) + f2d_bits(wl) : 0.0;
 }
+#elif FVS_DF
+// df64 value as FP64: two exact conversions on the integer pipe, one exact add
+__device__ __forceinline__ double to_double(df64 x) { return f2d_bits(x.hi) + f2d_bits(x.lo); }
+
+// df64 flux slots summed in df64 in the reference's order, times 1/vol in
+// df64, then one FP64 addition per component
+template <bool WS, bool COH>
+__device__ __forceinline__ void cell_residual(const DevView& d, int ic, double* res, double& ws) {
+  df64 r[4] = {df64(0.f, 0.f), df64(0.f, 0.f), df64(0.f, 0.f), df64(0.f, 0.f)}, w(0.f, 0.f);
+  const int4 cf = d.cflist[ic];
+  const int sl[4] = {cf.x, cf.y, cf.z, cf.w};
+#pragma unroll
+  for (int j = 0; j < 4; j++) {
+    const int s = sl[j];
+    if (s == 0) continue;
+    const int idx = (s > 0 ? s : -s) - 1;
+    df64 f[4];
+    ldc4<COH>(static_cast<const df64*>(d.eflux), idx, f);
+#pragma unroll
+    for (int v = 0; v < 4; v++) r[v] = s > 0 ? r[v] + f[v] : r[v] - f[v];
+    if (WS) w = w + ldc1<COH>(static_cast<const df64*>(d.ews), idx);
+  }
+  const df64 rv = -static_cast<const df64*>(d.volT)[ic];
+#pragma unroll
+  for (int v = 0; v < 4; v++) res[v] = to_double(r[v] * rv);
+  ws = WS ? to_double(w) : 0.0;
+}
 #else
 template <bool WS, bool COH>
 __device__ __forceinline__ void gather_slot(const DevView& d, int s, double* r, double& ws) {
@@ -569,6 +642,12 @@ __device__ __forceinline__ void cons2prim(T g, const double* u, T* p) {
   p[1] = d2f_bits(u[1]) * ri;
   p[2] = d2f_bits(u[2]) * ri;
   p[3] = g * (d2f_bits(u[3]) - 0.5f * r * (p[1] * p[1] + p[2] * p[2]));
+#elif FVS_DF
+  const df64 r = df_from_double(u[0]), ri = df64(1) / r;
+  p[0] = r;
+  p[1] = df_from_double(u[1]) * ri;
+  p[2] = df_from_double(u[2]) * ri;
+  p[3] = g * (df_from_double(u[3]) - df64(0.5) * r * (p[1] * p[1] + p[2] * p[2]));
 #elif !FVS_STRICT
   const double ri = 1.0 / u[0];
   p[0] = u[0];

@@ -77,6 +77,11 @@ def free_stream_state(c: Case, ncells: int, gamma: float = 1.4) -> np.ndarray:
     return np.tile(np.array([rho, rho * u, rho * v, e]), (ncells, 1))
 
 
+def free_stream_state_like(o, like: np.ndarray) -> np.ndarray:
+    """Free-stream state of options o with the shape of `like`."""
+    return free_stream_state(Case(0, 0, o.mach_inf, o.aoa_inf_deg), like.shape[0], o.gamma)
+
+
 def run_plain(cases, precision, max_steps, drop, starts=None, ref_levels=None, check_every=200, states=None,
               meshes=None):
     """One Solver per case, one after the other (the plain path).  Returns

@@ -12,7 +12,10 @@ metric).  Runs entirely on the GPU through the C-ABI; prints one JSON object.
                      defect-correction iteration (FP64 residual once per chunk,
                      FP32 linearised stages) to the target, confirmed by FP64
                      steps
-            learned  the same batch started from the network's prediction
+            learned  the same ladder started from the network's prediction
+            raced    every case started twice in one batch, from the
+                     prediction and from the free stream; the first twin to
+                     reach the target ends the pair
           errors: max |U - U_plain| / max|U_plain| of the final states, and
           the surrogate's error before any solver step
 """
@@ -24,7 +27,7 @@ import time
 import numpy as np
 
 from . import PREC_FP64, PREC_MIXED, sweep
-from .warmstart import WarmStart, build_dataset, reference_levels, solve_ladder
+from .warmstart import WarmStart, build_dataset, reference_levels, solve_ladder, solve_ladder_raced
 
 
 def run(n_train=96, n_test=24, wall=(64, 192), radial=(32, 96), max_steps=200000, epochs=30, seed_train=5,
@@ -61,6 +64,9 @@ def run(n_train=96, n_test=24, wall=(64, 192), radial=(32, 96), max_steps=200000
     starts = [ws.predict_state(c, m) for c, m in zip(test, meshes)]
     st_l, l1, l2, t_learn, ph_l = solve_ladder(meshes, [sweep.case_options(c, PREC_MIXED) for c in test], levels, switch,
                                             drop, max_steps, starts=starts)
+    st_r, r1, r2, t_race, ph_r, winner = solve_ladder_raced(
+        meshes, [sweep.case_options(c, PREC_MIXED) for c in test], levels, starts, switch=switch, drop=drop,
+        max_steps=max_steps)
 
     def err(a, b):
         return float(max(np.abs(x - y).max() / np.abs(y).max() for x, y in zip(a, b)))
@@ -81,8 +87,13 @@ def run(n_train=96, n_test=24, wall=(64, 192), radial=(32, 96), max_steps=200000
         "learned_batched_ladder": {"seconds": round(t_learn, 3), "steps_mixed": int(l1.max()), "steps_after_switch": int(l2.max()),
                                    "linf_vs_plain": err(st_l, plain_states),
                                    "phase_seconds": {k: round(v, 3) for k, v in ph_l.items()}},
+        "learned_raced_ladder": {"seconds": round(t_race, 3), "steps_mixed": int(r1.max()),
+                                 "steps_after_switch": int(r2.max()), "linf_vs_plain": err(st_r, plain_states),
+                                 "phase_seconds": {k: round(v, 3) for k, v in ph_r.items()}},
         "speedup_batched_vs_plain": round(t_plain / t_batch, 2),
         "speedup_learned_vs_plain": round(t_plain / t_learn, 2),
+        "speedup_learned_raced_vs_plain": round(t_plain / t_race, 2),
+        "steps_total": {"plain": int(steps_p.sum()), "batched": int((b1 + b2).sum()), "learned": int((l1 + l2).sum())},
         "surrogate_error": {"linf_rel": sur_inf, "l2_rel": sur_l2, "free_stream_linf_rel": fs_inf},
         "cases": [[c.nw, c.nr, round(c.mach, 4), round(c.aoa, 3)] for c in test],
         "steps_per_case_plain": steps_p.tolist(),
@@ -90,7 +101,37 @@ def run(n_train=96, n_test=24, wall=(64, 192), radial=(32, 96), max_steps=200000
         "steps_per_case_batched": (b1 + b2).tolist(),
         "linf_per_case_batched": per_case(st_b, plain_states),
         "linf_per_case_learned": per_case(st_l, plain_states),
+        "raced_learned_start_won": [int(w == 0) for w in winner],
     }
+    return out
+
+
+def run_airfoil(nw=512, nr=256, mach=0.8, aoa=1.25, drop=1e-10, switch=1e-5, max_steps=400000):
+    """Steady transonic NACA0012 O-grid (512 x 256 nodes, 261,120 cells,
+    M 0.8, 1.25 deg) to a 1e-10 drop of every RMS(dU) component: the plain
+    FP64 solver against a batch of one on the precision ladder with the
+    defect-correction phase.  First-order reconstruction: the reference's
+    second-order Venkatakrishnan scheme stalls on this mesh."""
+    from .solver import Solver
+    case = sweep.Case(nw, nr, mach, aoa)
+    mesh = case.mesh()
+    levels = reference_levels([case], [mesh])
+    out = {"workload": f"NACA0012 O-grid {nw}x{nr} nodes, {mesh.ncells} cells, M {mach}, AoA {aoa} deg, steady "
+                       "SSP-RK(4,2), local dt CFL 1.25, first-order Roe, slip wall + free stream",
+           "target": f"RMS(dU_k) <= {drop:g} x first-step RMS(dU_k) of the free-stream start, k = 1..4"}
+    t0 = time.perf_counter()
+    with Solver(mesh, sweep.case_options(case, PREC_FP64)) as s:
+        s.initialize_solution()
+        n_plain, _ = sweep._run_absolute(s, max_steps, drop, levels[0], 1000)
+        u_plain = s.cvar
+    t_plain = time.perf_counter() - t0
+    st, n1, n2, t_lad, ph = solve_ladder([mesh], [sweep.case_options(case, PREC_MIXED)], levels, switch, drop, max_steps,
+                                         chunk=500)
+    out["plain_fp64"] = {"seconds": round(t_plain, 3), "steps": int(n_plain)}
+    out["ladder_dc"] = {"seconds": round(t_lad, 3), "steps_mixed": int(n1[0]), "steps_after_switch": int(n2[0]),
+                        "phase_seconds": {k: round(v, 3) for k, v in ph.items()},
+                        "linf_vs_plain": float(np.abs(st[0] - u_plain).max() / np.abs(u_plain).max())}
+    out["speedup"] = round(t_plain / t_lad, 2)
     return out
 
 

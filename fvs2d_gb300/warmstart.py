@@ -48,8 +48,33 @@ def targets(case: sweep.Case, cvar: np.ndarray) -> np.ndarray:
     return (cvar - sweep.free_stream_state(case, cvar.shape[0])).astype(np.float32)
 
 
+def solve_ladder_raced(meshes, opts_mixed, levels, starts, **kw):
+    """The ladder with every case started twice, from `starts` and from the
+    free stream, in one batch; the twin that reaches the final level first
+    ends its group (the free stream is the fallback of a poor prediction).
+    Returns (states, steps_mixed, steps after the switch, seconds, phases,
+    winner) with winner[c] = 0 for the given start, 1 for the free stream."""
+    n = len(meshes)
+    lv = np.asarray(levels, np.float64).reshape(n, 4)
+    fs = [sweep.free_stream_state_like(o, u) for o, u in zip(opts_mixed, starts)]
+    states, n1, n2, secs, phases, done_last = solve_ladder(
+        list(meshes) + list(meshes), list(opts_mixed) + list(opts_mixed), np.concatenate([lv, lv]),
+        starts=list(starts) + fs, groups=list(range(n)) * 2, _return_last=True, **kw)
+    last = done_last
+    ok = np.all(last <= np.concatenate([lv, lv]) * kw.get("drop", 1e-10) * (1 + 1e-12), axis=1)
+    tot = n1 + n2
+    winner = np.zeros(n, np.int32)
+    for c in range(n):
+        a, b = (ok[c], tot[c]), (ok[c + n], tot[c + n])
+        if b[0] and (not a[0] or b[1] < a[1]):
+            winner[c] = 1
+    pick = [states[c + n * winner[c]] for c in range(n)]
+    return (pick, np.array([n1[c + n * winner[c]] for c in range(n)]),
+            np.array([n2[c + n * winner[c]] for c in range(n)]), secs, phases, winner)
+
+
 def solve_ladder(meshes, opts_mixed, levels, switch=1e-5, drop=1e-10, max_steps=200000, chunk=200, starts=None,
-                 autotune=True, dc=True):
+                 autotune=True, dc=True, groups=None, _return_last=False):
     """Batched precision-ladder solve to levels*drop (levels: per-case
     reference residuals [ncases][4]): mixed precision to levels*switch, then
     (dc) the defect-correction iteration to levels*drop followed by the FP64
@@ -72,6 +97,8 @@ def solve_ladder(meshes, opts_mixed, levels, switch=1e-5, drop=1e-10, max_steps=
         t3 = time.perf_counter()
         phases["mixed"] = t3 - t2
         n2 = np.zeros_like(n1)
+        if groups is not None:
+            b.set_groups(groups)
         if dc:
             n2, _, _, _ = b.run_to_level(max_steps, np.asarray(levels) * drop, chunk, dc=True)
             t4 = time.perf_counter()
@@ -82,6 +109,8 @@ def solve_ladder(meshes, opts_mixed, levels, switch=1e-5, drop=1e-10, max_steps=
         n2 = n2 + n3
         phases["fp64"] = time.perf_counter() - t3
         states = [b.get_state(c) for c in range(b.ncases)]
+    if _return_last:
+        return states, n1, n2, time.perf_counter() - t0, phases, last
     return states, n1, n2, time.perf_counter() - t0, phases
 
 

@@ -68,10 +68,15 @@ extern "C" {
  *              -ffp-contract=off wherever no transcendental is involved.
  * FP64:        same operations, FMA contraction allowed (fast FP64 drop-in).
  * MIXED:       gradients, limiter, reconstruction and flux in FP32; residual
- *              accumulation, state update, LSQ setup and norms in FP64.      */
+ *              accumulation, state update, LSQ setup and norms in FP64.
+ * FP64_DF:     gradients, limiter, reconstruction, flux and the residual
+ *              gather in double-float (pairs of FP32, 48-bit significand:
+ *              FP64-class accuracy on the FP32 pipe); FP64 state update,
+ *              local time step and norms.                                   */
 #define FVS_PREC_FP64_STRICT 0
 #define FVS_PREC_FP64        1
 #define FVS_PREC_MIXED       2
+#define FVS_PREC_FP64_DF     3
 
 /* ---- mesh: what grid_read / grid_bc_read load (src/grid_procs.f90:65-164) */
 typedef struct fvs_mesh {
@@ -249,6 +254,11 @@ int fvs_batch_set_precision(fvs_batch* b, int32_t precision);
 int fvs_batch_set_barrier_budget(fvs_batch* b, double seconds);
 /* nsteps (<= 1024) steps of every case; norms [ncases][nsteps][4] or NULL */
 int fvs_batch_steps(fvs_batch* b, int32_t nsteps, double* norms, float* ms);
+/* Groups of cases that stop together: when a case meets its target in a run
+ * below, the other active cases with the same group id stop at that step
+ * (several starts of one problem raced; the first to converge wins).
+ * group [ncases], or NULL: every case alone (the default). */
+int fvs_batch_set_groups(fvs_batch* b, const int32_t* group);
 /* steps until each case's RMS(dU) <= drop x its first value in all four
  * components; converged cases leave the work lists.  steps_done [ncases];
  * first, last [ncases][4] */

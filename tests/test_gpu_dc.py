@@ -71,3 +71,28 @@ def test_converges_to_the_fp64_fixed_point():
             s.cvar = states[c]
             r, _ = s.compute_residual(0.0)
         assert np.abs(r).max() <= 1e-7 * np.abs(r0).max(), (c, np.abs(r).max(), np.abs(r0).max())
+
+
+def test_groups_stop_together_and_pick_the_first():
+    meshes, opts = first_order_sweep(PREC_MIXED)
+    meshes, opts = meshes[:2] + meshes[:2], opts[:2] + opts[:2]
+    with Batch(meshes, opts) as b:
+        b.initialize_solution()
+        first, _ = b.steps(1)
+        levels = first[:, 0, :] * 1e-3
+        # twins 0/2 and 1/3: case 2 starts from a converged-ish state of case 0
+        b.initialize_solution()
+        b.run_to_level(100000, levels * 1e-2, chunk=50)
+        head = b.get_state(0)
+        b.initialize_solution()
+        b.set_state(2, head)
+        b.set_groups([0, 1, 0, 1])
+        done, _, last, _ = b.run_to_level(100000, levels, chunk=7)
+        b.set_groups(None)
+    # the warm twin met the target and ended the cold one at the same step
+    assert done[0] == done[2]
+    assert np.all(last[2] <= levels[2])
+    assert not np.all(last[0] <= levels[0])
+    # identical twins converge on the same step
+    assert done[1] == done[3]
+    assert np.all(last[1] <= levels[1]) and np.all(last[3] <= levels[3])
