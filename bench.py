@@ -136,6 +136,19 @@ def traffic_from_profile(kernel: str):
     return None
 
 
+def pipe_note(kernel: str):
+    """The compute pipe that binds a kernel, from the committed ncu summary
+    (the fourth column of profiles/ncu_traffic.txt, when present)."""
+    path = os.path.join(ROOT, "profiles", "ncu_traffic.txt")
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        t = line.split(None, 3)
+        if len(t) >= 4 and not line.startswith("#") and t[0] == kernel:
+            return t[3].strip()
+    return None
+
+
 def algorithmic_bytes(kernel: str, ncells: int, nedges: int, tsize: int) -> float:
     """Compulsory bytes of one launch (every array read or written once).
 
@@ -213,6 +226,7 @@ def run_ours(args) -> dict:
                 "traffic": traffic, "alg_bytes_per_launch": alg, "mean_launch_ms": round(per_launch[dom], 4),
                 "kernel_share": {k: round(v / sum(total.values()), 4) for k, v in total.items()},
                 "step_bytes_model": "252 B per cell-stage (ideal fused LSQ-fn FP64 stage)",
+                "compute_bound": pipe_note(f"{dom}:{args.precision}"),
                 "step_frac_of_hbm": round(value / ws * 252 / (peak * 1e9), 4)}
 
     # end to end through the C-ABI with pinned host buffers
@@ -357,11 +371,18 @@ def main():
                          "1e-10 drop on the 261,120-cell NACA0012 O-grid, plain FP64 vs the ladder")
     ap.add_argument("--n-train", type=int, default=96)
     ap.add_argument("--n-test", type=int, default=24)
+    ap.add_argument("--full-size", action="store_true",
+                    help="sweep meshes from the full distribution (64-512 wall x 32-256 radial nodes) instead of "
+                         "64-192 x 32-96")
     args = ap.parse_args()
     if args.workload in ("sweep", "airfoil"):
         from fvs2d_gb300 import _build, sweep_bench
         _build.build()
-        out = sweep_bench.run(args.n_train, args.n_test) if args.workload == "sweep" else sweep_bench.run_airfoil()
+        if args.workload == "sweep":
+            sizes = dict(wall=(64, 512), radial=(32, 256), race=False) if args.full_size else {}
+            out = sweep_bench.run(args.n_train, args.n_test, **sizes)
+        else:
+            out = sweep_bench.run_airfoil()
         print(json.dumps(out), flush=True)
         return
     if args.warmup < 3 and args.impl == "ours":

@@ -33,7 +33,7 @@ UNITS = {
     "fvs_batch.cu": [],
     "fvs_mlp.cu": [],
 }
-HEADERS = ["fvs_internal.hpp", "fvs_kernels.cuh", "fvs_layout.hpp", "df64.cuh"]
+HEADERS = ["fvs_internal.hpp", "fvs_kernels.cuh", "fvs_layout.hpp", "df64.cuh", "fvs_tcgemm.cuh"]
 
 
 def nvcc() -> str:

@@ -108,6 +108,7 @@ SIGNATURES = {
                                          C.c_void_p, C.POINTER(C.c_float)]),
     "fvs_mlp_create": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_uint64, C.POINTER(C.c_void_p)]),
     "fvs_mlp_destroy": (None, [C.c_void_p]),
+    "fvs_mlp_set_engine": (C.c_int, [C.c_void_p, C.c_int32]),
     "fvs_mlp_last_error": (C.c_char_p, [C.c_void_p]),
     "fvs_mlp_num_params": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64)]),
     "fvs_mlp_get_params": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64]),

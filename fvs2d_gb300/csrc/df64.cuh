@@ -85,6 +85,7 @@ __device__ __forceinline__ df64 dsqrt_(df64 x) {
   return fast_two_sum(s, __fdiv_rn(r, 2.0f * s));
 }
 __device__ __forceinline__ df64 dabs_(df64 x) { return x.hi < 0.0f ? -x : x; }
+__device__ __forceinline__ df64 half(df64 x) { return df64(0.5f * x.hi, 0.5f * x.lo); }
 __device__ __forceinline__ bool operator<(df64 a, df64 b) { return a.hi < b.hi || (a.hi == b.hi && a.lo < b.lo); }
 __device__ __forceinline__ bool operator>(df64 a, df64 b) { return b < a; }
 

@@ -157,7 +157,9 @@ struct StageParams {
 
 // Software grid barrier of the persistent kernel.  Every wait is bounded by a
 // clock64() budget; a wait that runs out sets err, every block leaves at its
-// next barrier and the host reports FVS_ERR_TIMEOUT.
+// next barrier and the host reports FVS_ERR_TIMEOUT.  (A two-level variant,
+// blocks meeting first in 64 groups, measured 3-5 % slower on a 16-case
+// sweep: with at most a few hundred resident blocks one counter suffices.)
 struct GridBarrier {
   unsigned int count;
   unsigned int gen;

@@ -151,6 +151,9 @@ __device__ __forceinline__ double dsqrt_(double x) { return sqrt(x); }
 __device__ __forceinline__ float dsqrt_(float x) { return sqrtf(x); }
 __device__ __forceinline__ double dabs_(double x) { return fabs(x); }
 __device__ __forceinline__ float dabs_(float x) { return fabsf(x); }
+// x / 2 (exact): 0.5 * x in FP64 / FP32, a scaling of both words in df64
+__device__ __forceinline__ double half(double x) { return 0.5 * x; }
+__device__ __forceinline__ float half(float x) { return 0.5f * x; }
 
 // limiter, src/gradient_limiter.f90:103-134 (eps2 precomputed per cell)
 __device__ __forceinline__ T limiter_fn(int type, T a, T b, T eps2) {
@@ -232,15 +235,15 @@ __device__ __forceinline__ void roe_flux_fast_t(R gamma, R gm1, R igm1, const R*
   const R riL = R(1) / rhoL, riR = R(1) / rhoR;
   const R unL = uL * nx + vL * ny, unR = uR * nx + vR * ny;
   const R utL = uL * tx + vL * ty, utR = uR * tx + vR * ty;
-  const R HL = gamma * pL * riL * igm1 + R(0.5) * (uL * uL + vL * vL);
-  const R HR = gamma * pR * riR * igm1 + R(0.5) * (uR * uR + vR * vR);
+  const R HL = gamma * pL * riL * igm1 + half(uL * uL + vL * vL);
+  const R HR = gamma * pR * riR * igm1 + half(uR * uR + vR * vR);
   const R RT = dsqrt_(rhoR * riL);
   const R rho = RT * rhoL;
   const R i1 = R(1) / (R(1) + RT);
   const R u = (uL + RT * uR) * i1;
   const R v = (vL + RT * vR) * i1;
   const R H = (HL + RT * HR) * i1;
-  const R q2 = R(0.5) * (u * u + v * v);
+  const R q2 = half(u * u + v * v);
   const R a2 = gm1 * (H - q2);
   const R a = dsqrt_(a2);
   const R ia2 = R(1) / a2;
@@ -248,14 +251,14 @@ __device__ __forceinline__ void roe_flux_fast_t(R gamma, R gm1, R igm1, const R*
   const R ut = u * tx + v * ty;
   const R drho = rhoR - rhoL, dp = pR - pL, dun = unR - unL, dut = utR - utL;
   const R rad = rho * a * dun;
-  const R L0 = (dp - rad) * R(0.5) * ia2;
+  const R L0 = half(dp - rad) * ia2;
   const R L1 = rho * dut;
   const R L2 = drho - dp * ia2;
-  const R L3 = (dp + rad) * R(0.5) * ia2;
+  const R L3 = half(dp + rad) * ia2;
   R ws0 = dabs_(un - a), ws3 = dabs_(un + a);
   const R ws1 = dabs_(un);
-  if (ws0 < R(0.2)) ws0 = R(0.5) * (ws0 * ws0 * R(5) + R(0.2));
-  if (ws3 < R(0.2)) ws3 = R(0.5) * (ws3 * ws3 * R(5) + R(0.2));
+  if (ws0 < R(0.2)) ws0 = half(ws0 * ws0 * R(5) + R(0.2));
+  if (ws3 < R(0.2)) ws3 = half(ws3 * ws3 * R(5) + R(0.2));
   const R w0 = ws0 * L0, w1 = ws1 * L1, w2 = ws1 * L2, w3 = ws3 * L3;
   const R s03 = w0 + w3, s = s03 + w2, dw = (w3 - w0) * a;
   const R diss0 = s;
@@ -263,11 +266,11 @@ __device__ __forceinline__ void roe_flux_fast_t(R gamma, R gm1, R igm1, const R*
   const R diss2 = v * s + dw * ny + w1 * ty;
   const R diss3 = H * s03 + un * dw + w1 * ut + w2 * q2;
   const R mL = rhoL * unL, mR = rhoR * unR;
-  flux[0] = R(0.5) * (mL + mR - diss0);
-  flux[1] = R(0.5) * (mL * uL + mR * uR + (pL + pR) * nx - diss1);
-  flux[2] = R(0.5) * (mL * vL + mR * vR + (pL + pR) * ny - diss2);
-  flux[3] = R(0.5) * (mL * HL + mR * HR - diss3);
-  ws_max = R(0.5) * (ws1 + a);
+  flux[0] = half(mL + mR - diss0);
+  flux[1] = half(mL * uL + mR * uR + (pL + pR) * nx - diss1);
+  flux[2] = half(mL * vL + mR * vR + (pL + pR) * ny - diss2);
+  flux[3] = half(mL * HL + mR * HR - diss3);
+  ws_max = half(ws1 + a);
 }
 
 __device__ __forceinline__ void roe_flux_fast(T gamma, T gm1, T igm1, const T* pl, const T* pr, T nx, T ny, T* flux,
@@ -1009,6 +1012,7 @@ __device__ __forceinline__ Dual dsqrt_(Dual a) {
   return Dual(s, 0.5f * a.d / s);
 }
 __device__ __forceinline__ Dual dabs_(Dual a) { return a.v < 0.f ? -a : a; }
+__device__ __forceinline__ Dual half(Dual a) { return Dual(0.5f * a.v, 0.5f * a.d); }
 
 // J dU of one edge slot (first order: face states are the cell states),
 // times the face area, into the slot's flux record

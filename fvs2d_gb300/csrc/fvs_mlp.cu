@@ -4,7 +4,9 @@
 // Network: n_in -> width (GELU) -> ... -> width (GELU) -> n_out, `depth`
 // hidden layers.  Weights are kept in FP32 (Adam master copy) and rounded to
 // BF16 for every GEMM; activations enter the GEMMs in BF16; every GEMM
-// accumulates in FP32 on the tensor cores (mma.sync m16n8k16 bf16).
+// accumulates in FP32 on the tensor cores: tcgen05.mma with the accumulator in
+// tensor memory (fvs_tcgemm.cuh, the default engine), or the warp-level
+// mma.sync m16n8k16 kernel below (kept as the comparison engine).
 // Training: minibatch Adam on the mean squared error.
 //
 // GEMM convention: C[m][n] = sum_k A(m,k) B(n,k) (+ bias[n]); each operand is
@@ -27,6 +29,7 @@
 #include <vector>
 
 #include "../../include/fvs2d.h"
+#include "fvs_tcgemm.cuh"
 
 namespace {
 
@@ -185,13 +188,24 @@ __global__ void k_gelu_back(const float* __restrict__ dA, const float* __restric
   if (i < n) dZ[i] = __float2bfloat16(dA[i] * gelu_grad(Z[i]));
 }
 
-// bias gradient: column sums of a [n x cols] BF16 matrix (ld), one thread per column
-__global__ void k_colsum(const bf16* __restrict__ g, int n, int cols, int ld, float* __restrict__ out) {
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= cols) return;
+// bias gradient: column sums of a [n x cols] BF16 matrix (ld).  A block of
+// 32 x 32 threads takes 32 columns: each thread row sums every 32nd matrix
+// row, then the 32 partial sums of a column are added in a fixed order
+// (deterministic).
+__global__ void __launch_bounds__(1024) k_colsum(const bf16* __restrict__ g, int n, int cols, int ld,
+                                                 float* __restrict__ out) {
+  __shared__ float part[32][33];
+  const int c = blockIdx.x * 32 + threadIdx.x;
   float s = 0.f;
-  for (int r = 0; r < n; r++) s += __bfloat162float(g[(size_t)r * ld + c]);
-  out[c] = s;
+  if (c < cols)
+    for (int r = threadIdx.y; r < n; r += 32) s += __bfloat162float(g[(size_t)r * ld + c]);
+  part[threadIdx.y][threadIdx.x] = s;
+  __syncthreads();
+  if (threadIdx.y == 0 && c < cols) {
+    float t = 0.f;
+    for (int k = 0; k < 32; k++) t += part[k][threadIdx.x];
+    out[c] = t;
+  }
 }
 
 __global__ void k_adam(float* __restrict__ w, const float* __restrict__ g, float* __restrict__ m, float* __restrict__ v, size_t n,
@@ -232,6 +246,8 @@ struct fvs_mlp {
   bf16* dz2 = nullptr;
   float* da = nullptr;               // [cap][max dim]
   float* loss = nullptr;
+  int* gemm_err = nullptr;           // set by a tcgen05 GEMM whose bounded wait expired
+  int engine = 0;                    // 0: tcgen05, 1: mma.sync
   int step = 0;
   std::vector<void*> owned;
 
@@ -272,10 +288,25 @@ struct fvs_mlp {
 namespace {
 
 template <bool A_KM, bool B_KM>
-void gemm(cudaStream_t s, const bf16* A, int lda, const bf16* B, int ldb, int M, int N, int K, int epi, const float* bias,
-          float* C, int ldc, bf16* Cact, int ldact) {
+void gemm(const fvs_mlp* m, const bf16* A, int lda, const bf16* B, int ldb, int M, int N, int K, int epi,
+          const float* bias, float* C, int ldc, bf16* Cact, int ldact) {
+  if (m->engine == 0) {
+    dim3 grid((unsigned)((N + tc::BN - 1) / tc::BN), (unsigned)((M + tc::BM - 1) / tc::BM));
+    tc::k_gemm_tc<A_KM, B_KM><<<grid, tc::THREADS, tc::SMEM_BYTES, m->stream>>>(A, lda, B, ldb, M, N, K, epi, bias, C,
+                                                                              ldc, Cact, ldact, m->gemm_err);
+    return;
+  }
   dim3 grid((unsigned)((N + BN - 1) / BN), (unsigned)((M + BM - 1) / BM));
-  k_gemm<A_KM, B_KM><<<grid, GEMM_THREADS, 0, s>>>(A, lda, B, ldb, M, N, K, epi, bias, C, ldc, Cact, ldact);
+  k_gemm<A_KM, B_KM><<<grid, GEMM_THREADS, 0, m->stream>>>(A, lda, B, ldb, M, N, K, epi, bias, C, ldc, Cact, ldact);
+}
+
+// the tcgen05 GEMM uses 64 KB of dynamic shared memory
+bool tc_gemm_setup() {
+  const int b = tc::SMEM_BYTES;
+  return cudaFuncSetAttribute(tc::k_gemm_tc<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, b) == cudaSuccess &&
+         cudaFuncSetAttribute(tc::k_gemm_tc<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, b) == cudaSuccess &&
+         cudaFuncSetAttribute(tc::k_gemm_tc<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, b) == cudaSuccess &&
+         cudaFuncSetAttribute(tc::k_gemm_tc<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, b) == cudaSuccess;
 }
 
 void refresh_bf16(fvs_mlp* m) { k_f32_to_bf16<<<nblk(m->nparam), 256, 0, m->stream>>>(m->w, m->wb, m->nparam); }
@@ -284,7 +315,7 @@ void refresh_bf16(fvs_mlp* m) { k_f32_to_bf16<<<nblk(m->nparam), 256, 0, m->stre
 void forward(fvs_mlp* m, int n) {
   for (int l = 0; l < m->nl; l++) {
     const bool last = l == m->nl - 1;
-    gemm<true, true>(m->stream, m->act[l], m->din[l], m->wb + m->woff[l], m->din[l], n, m->dout[l], m->din[l],
+    gemm<true, true>(m, m->act[l], m->din[l], m->wb + m->woff[l], m->din[l], n, m->dout[l], m->din[l],
                      last ? EPI_BIAS_F32 : EPI_BIAS_GELU, m->w + m->boff[l], m->pre[l], m->dout[l], last ? nullptr : m->act[l + 1],
                      m->dout[l]);
   }
@@ -297,11 +328,11 @@ void backward(fvs_mlp* m, int n) {
   for (int l = m->nl - 1; l >= 0; l--) {
     const int di = m->din[l], dn = m->dout[l];
     // dW_l[n][k] = sum_m dZ[m][n] act_l[m][k]
-    gemm<false, false>(m->stream, dcur, dn, m->act[l], di, dn, di, n, EPI_F32, nullptr, m->g + m->woff[l], di, nullptr, 0);
-    k_colsum<<<nblk(dn, 128), 128, 0, m->stream>>>(dcur, n, dn, dn, m->g + m->boff[l]);
+    gemm<false, false>(m, dcur, dn, m->act[l], di, dn, di, n, EPI_F32, nullptr, m->g + m->woff[l], di, nullptr, 0);
+    k_colsum<<<(dn + 31) / 32, dim3(32, 32), 0, m->stream>>>(dcur, n, dn, dn, m->g + m->boff[l]);
     if (l == 0) break;
     // dA_{l}[m][k] = sum_n dZ[m][n] W_l[n][k]; dZ_{l-1} = dA * gelu'(pre_{l-1})
-    gemm<true, false>(m->stream, dcur, dn, m->wb + m->woff[l], di, n, di, dn, EPI_F32, nullptr, m->da, di, nullptr, 0);
+    gemm<true, false>(m, dcur, dn, m->wb + m->woff[l], di, n, di, dn, EPI_F32, nullptr, m->da, di, nullptr, 0);
     k_gelu_back<<<nblk((size_t)n * di), 256, 0, m->stream>>>(m->da, m->pre[l - 1], dnext, (size_t)n * di);
     std::swap(dcur, dnext);
   }
@@ -310,7 +341,12 @@ void backward(fvs_mlp* m, int n) {
 int check(fvs_mlp* m, const char* where) {
   cudaError_t e = cudaGetLastError();
   if (e == cudaSuccess) e = cudaStreamSynchronize(m->stream);
-  return e == cudaSuccess ? FVS_OK : m->fail(FVS_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+  if (e != cudaSuccess) return m->fail(FVS_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+  int flag = 0;
+  e = cudaMemcpy(&flag, m->gemm_err, sizeof flag, cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return m->fail(FVS_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+  if (flag) return m->fail(FVS_ERR_TIMEOUT, std::string(where) + ": a tensor-core GEMM wait ran out of its budget");
+  return FVS_OK;
 }
 
 }  // namespace
@@ -346,13 +382,18 @@ int fvs_mlp_create(int32_t n_in, int32_t width, int32_t depth, int32_t n_out, ui
     g_mlp_error = "cudaStreamCreate failed";
     return FVS_ERR_CUDA;
   }
+  if (!tc_gemm_setup()) {
+    g_mlp_error = "tensor-core GEMM setup (dynamic shared memory) failed";
+    return FVS_ERR_CUDA;
+  }
   m->w = m->dalloc<float>(off);
   m->g = m->dalloc<float>(off);
   m->am = m->dalloc<float>(off);
   m->av = m->dalloc<float>(off);
   m->wb = m->dalloc<bf16>(off);
   m->loss = m->dalloc<float>(4);
-  if (!m->w || !m->g || !m->am || !m->av || !m->wb || !m->loss) {
+  m->gemm_err = m->dalloc<int>(4);
+  if (!m->w || !m->g || !m->am || !m->av || !m->wb || !m->loss || !m->gemm_err) {
     g_mlp_error = "MLP device allocation failed";
     return FVS_ERR_NOMEM;
   }
@@ -388,6 +429,12 @@ int fvs_mlp_num_params(const fvs_mlp* m, int64_t* n) {
     s += (int64_t)i * o + o;
   }
   *n = s;
+  return FVS_OK;
+}
+
+int fvs_mlp_set_engine(fvs_mlp* m, int32_t engine) {
+  if (!m || engine < 0 || engine > 1) return FVS_ERR_INVALID;
+  m->engine = engine;
   return FVS_OK;
 }
 

@@ -35,6 +35,11 @@ class MLP:
         except Exception:
             pass
 
+    def set_engine(self, engine: str) -> None:
+        """GEMM engine: "tcgen05" (default; tensor-core MMA, accumulator in
+        tensor memory) or "mma.sync" (warp-level MMA)."""
+        self._check(self._lib.fvs_mlp_set_engine(self._h, {"tcgen05": 0, "mma.sync": 1}[engine]))
+
     def num_params(self) -> int:
         n = C.c_int64(0)
         self._check(self._lib.fvs_mlp_num_params(self._h, C.byref(n)))

@@ -30,8 +30,8 @@ from . import PREC_FP64, PREC_MIXED, sweep
 from .warmstart import WarmStart, build_dataset, reference_levels, solve_ladder, solve_ladder_raced
 
 
-def run(n_train=96, n_test=24, wall=(64, 192), radial=(32, 96), max_steps=200000, epochs=30, seed_train=5,
-        seed_test=6, drop=1e-10, switch=1e-5):
+def run(n_train=96, n_test=24, wall=(64, 192), radial=(32, 96), max_steps=400000, epochs=30, seed_train=5,
+        seed_test=6, drop=1e-10, switch=1e-5, race=True):
     out = {"distribution": {"wall": wall, "radial": radial, "mach": [0.3, 0.85], "aoa_deg": [-2, 4],
                             "n_train": n_train, "n_test": n_test, "seeds": [seed_train, seed_test]},
            "scheme": "steady SSP-RK(4,2), local dt CFL 1.25, first-order Roe (the reference's second-order "
@@ -64,9 +64,10 @@ def run(n_train=96, n_test=24, wall=(64, 192), radial=(32, 96), max_steps=200000
     starts = [ws.predict_state(c, m) for c, m in zip(test, meshes)]
     st_l, l1, l2, t_learn, ph_l = solve_ladder(meshes, [sweep.case_options(c, PREC_MIXED) for c in test], levels, switch,
                                             drop, max_steps, starts=starts)
-    st_r, r1, r2, t_race, ph_r, winner = solve_ladder_raced(
-        meshes, [sweep.case_options(c, PREC_MIXED) for c in test], levels, starts, switch=switch, drop=drop,
-        max_steps=max_steps)
+    if race:
+        st_r, r1, r2, t_race, ph_r, winner = solve_ladder_raced(
+            meshes, [sweep.case_options(c, PREC_MIXED) for c in test], levels, starts, switch=switch, drop=drop,
+            max_steps=max_steps)
 
     def err(a, b):
         return float(max(np.abs(x - y).max() / np.abs(y).max() for x, y in zip(a, b)))
@@ -87,12 +88,8 @@ def run(n_train=96, n_test=24, wall=(64, 192), radial=(32, 96), max_steps=200000
         "learned_batched_ladder": {"seconds": round(t_learn, 3), "steps_mixed": int(l1.max()), "steps_after_switch": int(l2.max()),
                                    "linf_vs_plain": err(st_l, plain_states),
                                    "phase_seconds": {k: round(v, 3) for k, v in ph_l.items()}},
-        "learned_raced_ladder": {"seconds": round(t_race, 3), "steps_mixed": int(r1.max()),
-                                 "steps_after_switch": int(r2.max()), "linf_vs_plain": err(st_r, plain_states),
-                                 "phase_seconds": {k: round(v, 3) for k, v in ph_r.items()}},
         "speedup_batched_vs_plain": round(t_plain / t_batch, 2),
         "speedup_learned_vs_plain": round(t_plain / t_learn, 2),
-        "speedup_learned_raced_vs_plain": round(t_plain / t_race, 2),
         "steps_total": {"plain": int(steps_p.sum()), "batched": int((b1 + b2).sum()), "learned": int((l1 + l2).sum())},
         "surrogate_error": {"linf_rel": sur_inf, "l2_rel": sur_l2, "free_stream_linf_rel": fs_inf},
         "cases": [[c.nw, c.nr, round(c.mach, 4), round(c.aoa, 3)] for c in test],
@@ -101,8 +98,13 @@ def run(n_train=96, n_test=24, wall=(64, 192), radial=(32, 96), max_steps=200000
         "steps_per_case_batched": (b1 + b2).tolist(),
         "linf_per_case_batched": per_case(st_b, plain_states),
         "linf_per_case_learned": per_case(st_l, plain_states),
-        "raced_learned_start_won": [int(w == 0) for w in winner],
     }
+    if race:
+        out["test"]["learned_raced_ladder"] = {
+            "seconds": round(t_race, 3), "steps_mixed": int(r1.max()), "steps_after_switch": int(r2.max()),
+            "linf_vs_plain": err(st_r, plain_states), "phase_seconds": {k: round(v, 3) for k, v in ph_r.items()},
+            "learned_start_won": [int(w == 0) for w in winner]}
+        out["test"]["speedup_learned_raced_vs_plain"] = round(t_plain / t_race, 2)
     return out
 
 

@@ -288,6 +288,9 @@ typedef struct fvs_mlp fvs_mlp;
 int fvs_mlp_create(int32_t n_in, int32_t width, int32_t depth, int32_t n_out, uint64_t seed, fvs_mlp** out);
 void fvs_mlp_destroy(fvs_mlp* m);
 const char* fvs_mlp_last_error(const fvs_mlp* m);
+/* GEMM engine: 0 = tcgen05 tensor-core MMA with the accumulator in tensor
+ * memory (default), 1 = warp-level mma.sync (the comparison engine) */
+int fvs_mlp_set_engine(fvs_mlp* m, int32_t engine);
 int fvs_mlp_num_params(const fvs_mlp* m, int64_t* n);
 int fvs_mlp_get_params(fvs_mlp* m, float* dst, int64_t n);
 int fvs_mlp_set_params(fvs_mlp* m, const float* src, int64_t n);

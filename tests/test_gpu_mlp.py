@@ -15,10 +15,12 @@ import mlp_oracle  # noqa: E402
 pytestmark = pytest.mark.gpu
 
 
+@pytest.mark.parametrize("engine", ["tcgen05", "mma.sync"])
 @pytest.mark.parametrize("n,n_in,width,depth,n_out", [(64, 5, 32, 2, 4), (300, 5, 256, 4, 4), (257, 7, 48, 1, 3)])
-def test_gradients_match_cpu_oracle(n, n_in, width, depth, n_out):
+def test_gradients_match_cpu_oracle(n, n_in, width, depth, n_out, engine):
     rng = np.random.default_rng(11)
     m = MLP(n_in, width, depth, n_out, seed=3)
+    m.set_engine(engine)
     x = rng.standard_normal((n, n_in)).astype(np.float32)
     y = rng.standard_normal((n, n_out)).astype(np.float32) * 0.3
     p = m.get_params()
@@ -58,3 +60,20 @@ def test_training_fits_smooth_target():
     pred = m.predict(x[:4096])
     mse = float(((pred - y[:4096]) ** 2).mean())
     assert mse < 0.02 * base and mse < 2e-3, (base, mse, losses)
+
+
+def test_engines_agree():
+    """tcgen05 and mma.sync multiply the same BF16 operands with FP32
+    accumulation; only the accumulation order differs."""
+    rng = np.random.default_rng(3)
+    x = rng.standard_normal((5000, 5)).astype(np.float32)
+    y = rng.standard_normal((5000, 4)).astype(np.float32)
+    m = MLP(5, 256, 4, 4, seed=7)
+    a = m.predict(x)
+    la, ga = m.loss_grad(x[:3000], y[:3000])
+    m.set_engine("mma.sync")
+    b = m.predict(x)
+    lb, gb = m.loss_grad(x[:3000], y[:3000])
+    assert np.abs(a - b).max() <= 1e-3 * np.abs(b).max(), np.abs(a - b).max()
+    assert abs(la - lb) <= 1e-4 * abs(lb)
+    assert np.linalg.norm(ga - gb) <= 1e-2 * np.linalg.norm(gb)
