@@ -686,6 +686,108 @@ __device__ __forceinline__ void block_sum4(const double* v, double* out) {
     for (int k = 0; k < 4; k++) out[k] = sh[k][0];
 }
 
+#if FVS_MIXED
+// Mixed precision: the slot sums are exact (TwoSum) and the state stays FP64,
+// but the RK increment h (c R + F) is formed in FP32 (relative error 2^-24
+// of the increment, below the FP32 flux rounding already in R) and added to
+// the FP64 state: 4-8 FP64 additions per cell and stage instead of ~30 FP64
+// operations.  The accumulator F is stored as FP32 (float4 per cell).
+__device__ __forceinline__ void cell_residual_f(const DevView& d, int ic, bool want_ws, float* res, float& ws) {
+  float hi[4] = {0.f, 0.f, 0.f, 0.f}, lo[4] = {0.f, 0.f, 0.f, 0.f}, wh = 0.f, wl = 0.f;
+  const int4 cf = d.cflist[ic];
+  const int sl[4] = {cf.x, cf.y, cf.z, cf.w};
+#pragma unroll
+  for (int j = 0; j < 4; j++) {
+    const int s = sl[j];
+    if (s == 0) continue;
+    const int idx = (s > 0 ? s : -s) - 1;
+    float f[4];
+    ldc4<true>(static_cast<const float*>(d.eflux), idx, f);
+#pragma unroll
+    for (int v = 0; v < 4; v++) two_sum(hi[v], lo[v], s > 0 ? f[v] : -f[v]);
+    if (want_ws) two_sum(wh, wl, ldc1<true>(static_cast<const float*>(d.ews), idx));
+  }
+  const float rv = -static_cast<const float*>(d.volT)[ic];
+#pragma unroll
+  for (int v = 0; v < 4; v++) res[v] = (hi[v] + lo[v]) * rv;
+  ws = wh + wl;
+}
+
+template <int MODE, bool COH>
+__device__ __forceinline__ void update_item(const DevView& d, const StageParams& sp, int ic, double* d2) {
+  float res[4], ws;
+  cell_residual_f(d, ic, sp.steady && sp.stage == 1, res, ws);
+  float h = float(sp.h);
+  if (sp.steady) {
+    float dtl;
+    if (sp.stage == 1) {  // compute_local_time, src/runge_kutta.f90:424-437
+      dtl = float(d.cfl) / (static_cast<const float*>(d.volT)[ic] * (0.5f * ws));
+      d.dtl[ic] = f2d_bits(dtl);
+    } else {
+      dtl = d2f_bits(ldc1<COH>(d.dtl, ic));
+    }
+    h = dtl * float(sp.cst);
+  }
+  float* F = reinterpret_cast<float*>(d.F);
+  double u0[4], u[4];
+  float f[4], inc[4];
+  if (sp.stage == 1) {
+    ldc4<COH>(d.U, ic, u0);
+    st4(d.U0, ic, u0);
+#pragma unroll
+    for (int v = 0; v < 4; v++) f[v] = 0.f;
+  } else {
+    ldc4<COH>(d.U0, ic, u0);
+    if (MODE != MODE_SSP3) ldc4<COH>(F, ic, f);
+  }
+  const float coef = float(sp.coef);
+  if (MODE == MODE_SSP42) {
+    // src/runge_kutta.f90:225-226 / :383-387
+#pragma unroll
+    for (int v = 0; v < 4; v++) {
+      inc[v] = h * (coef * res[v] + f[v]);
+      f[v] = f[v] + res[v];
+      u[v] = u0[v] + f2d_bits(inc[v]);
+    }
+    if (!sp.last) st4(F, ic, f);
+  } else if (MODE == MODE_RK) {
+    // src/runge_kutta.f90:156-162 / :302-313
+#pragma unroll
+    for (int v = 0; v < 4; v++) {
+      f[v] = f[v] + coef * res[v];
+      inc[v] = sp.last ? h * f[v] : h * res[v];
+      u[v] = u0[v] + f2d_bits(inc[v]);
+    }
+    if (!sp.last) st4(F, ic, f);
+  } else {
+    // SSP-RK3 (Shu-Osher): u = a u0 + b (cur + h R) = u0 + b ((cur - u0) + h R)
+    if (sp.stage == 1) {
+#pragma unroll
+      for (int v = 0; v < 4; v++) {
+        inc[v] = h * res[v];
+        u[v] = u0[v] + f2d_bits(inc[v]);
+      }
+    } else {
+      double cur[4];
+      ldc4<COH>(d.U, ic, cur);
+      const float b = float(sp.b);
+#pragma unroll
+      for (int v = 0; v < 4; v++) {
+        inc[v] = b * (d2f_bits(cur[v] - u0[v]) + h * res[v]);
+        u[v] = u0[v] + f2d_bits(inc[v]);
+      }
+    }
+  }
+  st4(d.U, ic, u);
+  T p[4];
+  cons2prim(TP(gm1), u, p);
+  st4(static_cast<T*>(d.Pv), ic, p);
+  if (sp.last) {
+#pragma unroll
+    for (int v = 0; v < 4; v++) d2[v] += f2d_bits(inc[v] * inc[v]);
+  }
+}
+#else
 // one cell of an RK stage; at the last stage adds |U-U0|^2 to d2
 template <int MODE, bool COH>
 __device__ __forceinline__ void update_item(const DevView& d, const StageParams& sp, int ic, double* d2) {
@@ -758,6 +860,8 @@ __device__ __forceinline__ void update_item(const DevView& d, const StageParams&
     }
   }
 }
+
+#endif  // FVS_MIXED
 
 template <int MODE>
 __global__ void __launch_bounds__(256) k_update(const DevView d, const StageParams sp) {
