@@ -207,12 +207,13 @@ void enqueue_step(fvs_handle* H) {
     K.flux(H->d, sp.dts, s);
     K.update(H->d, sp, s);
   }
-  K.norm_final(H->d, s);
 }
 
 int count_launches(const fvs_handle* H) {
+  // k_begin_step, then gradient (second order), flux and update per stage;
+  // the last update also reduces the norms
   int per_stage = (H->d.first_order ? 0 : 1) + 2;
-  return 2 + per_stage * (int)H->stages.size();
+  return 1 + per_stage * (int)H->stages.size();
 }
 
 int ensure_graph(fvs_handle* H, int steps_per_graph) {
@@ -534,9 +535,10 @@ static int run_steps(fvs_handle* h, double t1, int nsteps, double* resnorm, floa
   if ((rc = ensure_graph(h, 1))) return rc;
   // control words: t1, steps done = 0
   h->h_small[0] = t1;
-  reinterpret_cast<int*>(h->h_small + 1)[0] = 0;
+  reinterpret_cast<int*>(h->h_small + 1)[0] = 0;  // steps done
+  reinterpret_cast<int*>(h->h_small + 1)[1] = 0;  // blocks done in the current last stage
   cudaError_t e = cudaMemcpyAsync(h->d.tctl, h->h_small, sizeof(double), cudaMemcpyHostToDevice, h->stream);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(h->d.stepctl, h->h_small + 1, sizeof(int), cudaMemcpyHostToDevice, h->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(h->d.stepctl, h->h_small + 1, 2 * sizeof(int), cudaMemcpyHostToDevice, h->stream);
   if (e != cudaSuccess) return h->cuda_fail(e, "step control upload");
   if (ms) cudaEventRecord(h->ev0, h->stream);
   const int cap = h->d.norm_cap;
@@ -725,8 +727,6 @@ int fvs_profile_step(fvs_handle* h, int32_t cap, int32_t* n, char* names, float*
     K.update(h->d, sp, s);
     mark("update");
   }
-  K.norm_final(h->d, s);
-  mark("norm");
   cudaError_t e = cudaStreamSynchronize(s);
   if (e != cudaSuccess) return h->cuda_fail(e, "profile step");
   int m = 0;

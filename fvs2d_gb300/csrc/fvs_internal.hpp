@@ -199,7 +199,6 @@ struct KernelSet {
   void (*flux)(const DevView&, double dts, cudaStream_t);
   void (*update)(const DevView&, const StageParams&, cudaStream_t);
   void (*residual_out)(const DevView&, cudaStream_t);
-  void (*norm_final)(const DevView&, cudaStream_t);
   // persistent kernel (LSQ gradients): resident blocks per SM for a block
   // size (0: the scheme has no persistent variant), and the cooperative launch
   int (*persistent_occupancy)(const DevView&, int block);

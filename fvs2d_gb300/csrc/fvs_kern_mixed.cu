@@ -9,8 +9,7 @@
 namespace fvs {
 const KernelSet& kernels_mixed() {
   static const KernelSet k = {"mixed", k_mixed::launch_begin_step, k_mixed::launch_cvar2pvar, k_mixed::launch_gradient,
-                              k_mixed::launch_flux, k_mixed::launch_update, k_mixed::launch_residual_out,
-                              k_mixed::launch_norm_final, k_mixed::persistent_occupancy,
+                              k_mixed::launch_flux, k_mixed::launch_update, k_mixed::launch_residual_out, k_mixed::persistent_occupancy,
                               k_mixed::launch_persistent};
   return k;
 }

@@ -863,17 +863,48 @@ __device__ __forceinline__ void update_item(const DevView& d, const StageParams&
 
 #endif  // FVS_MIXED
 
+// RMS of |U - U0| per component from the block partials, by one block of
+// 256 threads in a fixed order (deterministic); advances the step counter
+__device__ __forceinline__ void norm_final_block(const DevView& d) {
+  double s[4] = {0.0, 0.0, 0.0, 0.0};
+  for (int i = threadIdx.x; i < d.nblk_red; i += blockDim.x)
+#pragma unroll
+    for (int k = 0; k < 4; k++) s[k] += __ldcg(d.partials + 4 * i + k);
+  double out[4];
+  block_sum4(s, out);
+  if (threadIdx.x == 0) {
+    const int istep = d.stepctl[0] + 1;
+    double* o = d.norms + 4 * (size_t)((istep - 1) % d.norm_cap);
+#pragma unroll
+    for (int k = 0; k < 4; k++) o[k] = sqrt(out[k] / double(d.nc));
+    d.stepctl[0] = istep;
+  }
+}
+
+// One RK stage over all cells.  At the last stage every block writes its
+// partial norms; the block that finishes last (a counter in stepctl[1])
+// reduces them, so no separate norm launch is needed.
 template <int MODE>
 __global__ void __launch_bounds__(256) k_update(const DevView d, const StageParams sp) {
   const int ic = blockIdx.x * blockDim.x + threadIdx.x;
   double d2[4] = {0.0, 0.0, 0.0, 0.0};
   if (ic < d.nc) update_item<MODE, false>(d, sp, ic, d2);
   if (sp.last) {
+    __shared__ int s_last;
     double out[4];
     block_sum4(d2, out);
-    if (threadIdx.x == 0)
+    if (threadIdx.x == 0) {
 #pragma unroll
       for (int k = 0; k < 4; k++) d.partials[4 * blockIdx.x + k] = out[k];
+      __threadfence();
+      s_last = atomicAdd(&d.stepctl[1], 1) == (int)gridDim.x - 1;
+    }
+    __syncthreads();
+    if (s_last) {
+      __threadfence();
+      norm_final_block(d);
+      if (threadIdx.x == 0) d.stepctl[1] = 0;
+    }
   }
 }
 
@@ -903,23 +934,6 @@ __global__ void k_begin_step(const DevView d) {
   d.tctl[1] = d.tctl[0] + double(istep - 1) * d.dt;
 }
 
-// RMS of |U - U0| per component from the block partials: one block,
-// fixed-order sums (deterministic)
-__global__ void __launch_bounds__(256) k_norm_final(const DevView d) {
-  double s[4] = {0.0, 0.0, 0.0, 0.0};
-  for (int i = threadIdx.x; i < d.nblk_red; i += blockDim.x)
-#pragma unroll
-    for (int k = 0; k < 4; k++) s[k] += d.partials[4 * i + k];
-  double out[4];
-  block_sum4(s, out);
-  if (threadIdx.x == 0) {
-    const int istep = d.stepctl[0] + 1;
-    double* o = d.norms + 4 * (size_t)((istep - 1) % d.norm_cap);
-#pragma unroll
-    for (int k = 0; k < 4; k++) o[k] = sqrt(out[k] / double(d.nc));
-    d.stepctl[0] = istep;
-  }
-}
 
 // ---------------------------------------------------------------------------
 // persistent kernel: whole RK steps in one cooperative launch
@@ -1088,7 +1102,6 @@ static void launch_update(const DevView& d, const StageParams& sp, cudaStream_t 
 }
 
 static void launch_residual_out(const DevView& d, cudaStream_t s) { k_residual_out<<<grid_of(d.nc), 256, 0, s>>>(d); }
-static void launch_norm_final(const DevView& d, cudaStream_t s) { k_norm_final<<<1, 256, 0, s>>>(d); }
 
 #if FVS_MIXED
 // ---------------------------------------------------------------------------
