@@ -247,6 +247,8 @@ struct fvs_mlp {
   float* da = nullptr;               // [cap][max dim]
   float* loss = nullptr;
   int* gemm_err = nullptr;           // set by a tcgen05 GEMM whose bounded wait expired
+  float* split_ws = nullptr;         // split-K partial sums of the tcgen05 GEMM
+  size_t split_cap = 0;              // floats
   int engine = 0;                    // 0: tcgen05, 1: mma.sync
   int step = 0;
   std::vector<void*> owned;
@@ -288,12 +290,37 @@ struct fvs_mlp {
 namespace {
 
 template <bool A_KM, bool B_KM>
-void gemm(const fvs_mlp* m, const bf16* A, int lda, const bf16* B, int ldb, int M, int N, int K, int epi,
+void gemm(fvs_mlp* m, const bf16* A, int lda, const bf16* B, int ldb, int M, int N, int K, int epi,
           const float* bias, float* C, int ldc, bf16* Cact, int ldact) {
   if (m->engine == 0) {
-    dim3 grid((unsigned)((N + tc::BN - 1) / tc::BN), (unsigned)((M + tc::BM - 1) / tc::BM));
-    tc::k_gemm_tc<A_KM, B_KM><<<grid, tc::THREADS, tc::SMEM_BYTES, m->stream>>>(A, lda, B, ldb, M, N, K, epi, bias, C,
-                                                                              ldc, Cact, ldact, m->gemm_err);
+    const int tiles = ((N + tc::BN - 1) / tc::BN) * ((M + tc::BM - 1) / tc::BM);
+    const int nk = (K + tc::BK - 1) / tc::BK;
+    int nsplit = 1;
+    if (epi == EPI_F32 && C && !Cact && tiles < 64 && nk >= 4) {
+      // few output tiles and a long K (the weight gradient, K = batch rows):
+      // split K so that about one CTA per SM works, then add the partials
+      const int want = std::max(1, 148 / tiles);
+      const int per = std::max(1, (nk + want - 1) / want);
+      nsplit = (nk + per - 1) / per;
+      const size_t need = (size_t)nsplit * M * ldc;
+      if (nsplit > 1 && need > m->split_cap) {
+        float* w = m->dalloc<float>(need);
+        if (w) {
+          m->split_ws = w;
+          m->split_cap = need;
+        } else {
+          nsplit = 1;
+        }
+      }
+    }
+    dim3 grid((unsigned)((N + tc::BN - 1) / tc::BN), (unsigned)((M + tc::BM - 1) / tc::BM), (unsigned)nsplit);
+    const size_t stride = (size_t)M * ldc;
+    float* out = nsplit > 1 ? m->split_ws : C;
+    tc::k_gemm_tc<A_KM, B_KM><<<grid, tc::THREADS, tc::SMEM_BYTES, m->stream>>>(A, lda, B, ldb, M, N, K, epi, bias,
+                                                                              out, ldc, Cact, ldact, m->gemm_err,
+                                                                              stride);
+    if (nsplit > 1)
+      tc::k_sum_splits<<<nblk((size_t)M * N), 256, 0, m->stream>>>(m->split_ws, nsplit, stride, M, N, ldc, C);
     return;
   }
   dim3 grid((unsigned)((N + BN - 1) / BN), (unsigned)((M + BM - 1) / BM));

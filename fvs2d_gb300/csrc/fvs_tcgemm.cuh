@@ -14,7 +14,12 @@
 //     N 128, K 16) and commits them to the stage's mbarrier, which frees the
 //     stage for the block two steps later;
 //   - after the last block, warp w reads accumulator rows 32w..32w+31
-//     (tensor-memory lanes) with tcgen05.ld and applies the epilogue.
+//     (tensor-memory lanes) with tcgen05.ld, 32 columns at a time, transposes
+//     them through shared memory and writes whole row segments (coalesced)
+//     with the epilogue applied.
+// Split K (gridDim.z > 1): CTA z sums its own range of K blocks into the
+// partial matrix C + z * split_stride (raw accumulators, no epilogue);
+// k_sum_splits adds the partials in order (deterministic).
 // Every mbarrier wait is bounded (clock64 budget).  On expiry the kernel sets
 // *err, waits (bounded) for the MMAs it issued, frees its tensor memory and
 // returns.
@@ -134,7 +139,8 @@ template <bool A_KM, bool B_KM>
 __global__ void __launch_bounds__(THREADS) k_gemm_tc(const bf16* __restrict__ A, int lda, const bf16* __restrict__ B,
                                                      int ldb, int M, int N, int K, int epi,
                                                      const float* __restrict__ bias, float* __restrict__ C, int ldc,
-                                                     bf16* __restrict__ Cact, int ldact, int* __restrict__ err) {
+                                                     bf16* __restrict__ Cact, int ldact, int* __restrict__ err,
+                                                     size_t split_stride) {
   extern __shared__ __align__(128) uint8_t smem[];
   __shared__ __align__(8) uint64_t mbar[STAGES];
   __shared__ uint32_t tmem_slot;
@@ -162,7 +168,12 @@ __global__ void __launch_bounds__(THREADS) k_gemm_tc(const bf16* __restrict__ A,
   asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
   const uint32_t tmem = tmem_slot;
 
-  const int nk = (K + BK - 1) / BK;
+  // K blocks of this CTA (all of them without split K)
+  const int nk_all = (K + BK - 1) / BK;
+  const int per = (nk_all + (int)gridDim.z - 1) / (int)gridDim.z;
+  const int kb0 = (int)blockIdx.z * per;
+  const int nk = max(0, min(nk_all - kb0, per));
+  if (gridDim.z > 1) C += (size_t)blockIdx.z * split_stride;
   int issued = -1;  // last K block whose MMAs thread 0 committed
   for (int kb = 0; kb < nk; kb++) {
     const int s = kb & 1;
@@ -172,8 +183,8 @@ __global__ void __launch_bounds__(THREADS) k_gemm_tc(const bf16* __restrict__ A,
       __syncthreads();
       if (!s_ok) break;
     }
-    stage_tile<A_KM>(sA[s], A, lda, m0, M, kb * BK, K);
-    stage_tile<B_KM>(sB[s], B, ldb, n0, N, kb * BK, K);
+    stage_tile<A_KM>(sA[s], A, lda, m0, M, (kb0 + kb) * BK, K);
+    stage_tile<B_KM>(sB[s], B, ldb, n0, N, (kb0 + kb) * BK, K);
     asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
     __syncthreads();
     if (tid == 0) {
@@ -202,7 +213,9 @@ __global__ void __launch_bounds__(THREADS) k_gemm_tc(const bf16* __restrict__ A,
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
   if (s_ok) {
-    const int m = m0 + warp * 32 + lane;
+    // transpose staging, one 32 x 33 float tile per warp, in the (now free)
+    // operand stages
+    float* st = reinterpret_cast<float*>(smem) + warp * (32 * 33);
 #pragma unroll 1
     for (int c0 = 0; c0 < BN; c0 += 32) {
       uint32_t v[32];
@@ -217,17 +230,26 @@ __global__ void __launch_bounds__(THREADS) k_gemm_tc(const bf16* __restrict__ A,
           : "r"(taddr)
           : "memory");
       asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
-      if (m < M) {
+      // lane = row: v[j] is column c0 + j; write the tile, read it back by
+      // column so that each store instruction covers 32 consecutive columns
+      if (nk == 0) {
 #pragma unroll
-        for (int j = 0; j < 32; j++) {
-          const int n = n0 + c0 + j;
-          if (n >= N) break;
-          float z = __uint_as_float(v[j]);
-          if (epi != 0 && bias) z += bias[n];
-          if (C) C[(size_t)m * ldc + n] = z;
-          if (epi == 2 && Cact) Cact[(size_t)m * ldact + n] = __float2bfloat16(gelu_tc(z));
-        }
+        for (int j = 0; j < 32; j++) v[j] = 0u;  // an empty K range contributes zeros
       }
+#pragma unroll
+      for (int j = 0; j < 32; j++) st[lane * 33 + j] = __uint_as_float(v[j]);
+      __syncwarp();
+      const int n = n0 + c0 + lane;
+      const float bn = (epi != 0 && bias && n < N) ? bias[n] : 0.f;
+#pragma unroll 4
+      for (int r = 0; r < 32; r++) {
+        const int m = m0 + warp * 32 + r;
+        if (m >= M || n >= N) continue;
+        const float z = st[r * 33 + lane] + bn;
+        if (C) C[(size_t)m * ldc + n] = z;
+        if (epi == 2 && Cact) Cact[(size_t)m * ldact + n] = __float2bfloat16(gelu_tc(z));
+      }
+      __syncwarp();
     }
   } else if (tid == 0) {
     atomicExch(err, 1);
@@ -237,6 +259,19 @@ __global__ void __launch_bounds__(THREADS) k_gemm_tc(const bf16* __restrict__ A,
   if (warp == 0) {
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
   }
+}
+
+// C[m][n] = sum over z of the split partials P[z][m][n] (ldc, stride), in
+// order z = 0, 1, ... (deterministic)
+__global__ void k_sum_splits(const float* __restrict__ P, int nsplit, size_t stride, int M, int N, int ldc,
+                             float* __restrict__ C) {
+  const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i >= (size_t)M * N) return;
+  const int m = (int)(i / N), n = (int)(i % N);
+  const size_t o = (size_t)m * ldc + n;
+  float acc = 0.f;
+  for (int z = 0; z < nsplit; z++) acc += P[z * stride + o];
+  C[o] = acc;
 }
 
 }  // namespace tc

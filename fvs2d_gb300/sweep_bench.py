@@ -137,13 +137,40 @@ def run_airfoil(nw=512, nr=256, mach=0.8, aoa=1.25, drop=1e-10, switch=1e-5, max
     return out
 
 
+def profile_batch(ncases=16, steps=400, chunk=200):
+    """A fixed amount of batched work for kernel profiling: the 16-case reduced
+    sweep (261,780 cells), `steps` mixed persistent steps, then `steps`
+    defect-correction steps, in chunks of `chunk` (one cooperative launch
+    each).  Returns the per-phase seconds."""
+    from .batch import Batch
+    cases = sweep.draw_cases(ncases, 6, (64, 192), (32, 96))
+    meshes = [c.mesh() for c in cases]
+    never = np.zeros((ncases, 4))
+    out = {"cells": int(sum(m.ncells for m in meshes)), "steps": steps, "chunk": chunk}
+    with Batch(meshes, [sweep.case_options(c, PREC_MIXED) for c in cases]) as b:
+        b.initialize_solution()
+        t0 = time.perf_counter()
+        b.run_to_level(steps, never, chunk)
+        t1 = time.perf_counter()
+        b.run_to_level(steps, never, chunk, dc=True)
+        t2 = time.perf_counter()
+    out["mixed_seconds"] = round(t1 - t0, 4)
+    out["dc_seconds"] = round(t2 - t1, 4)
+    return out
+
+
 def main(argv=None):
     import argparse
     ap = argparse.ArgumentParser()
     ap.add_argument("--n-train", type=int, default=96)
     ap.add_argument("--n-test", type=int, default=24)
     ap.add_argument("--epochs", type=int, default=30)
+    ap.add_argument("--profile-batch", action="store_true",
+                    help="a fixed 16-case batched run (400 mixed + 400 defect-correction steps) for ncu")
     a = ap.parse_args(argv)
+    if a.profile_batch:
+        print(json.dumps(profile_batch()), flush=True)
+        return
     print(json.dumps(run(a.n_train, a.n_test, epochs=a.epochs)), flush=True)
 
 
