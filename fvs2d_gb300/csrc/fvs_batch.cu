@@ -730,12 +730,12 @@ int fvs_batch_run_to_level_dc(fvs_batch* b, int32_t max_steps, const double* lev
   DevView& d64 = b->d;
   const size_t n4 = 16 * (size_t)b->nc;
   if (!b->dc.D) {
-    void* p[5];
-    for (int k = 0; k < 5; k++)
-      if (!b->arena.alloc(p[k], n4)) return b->fail(FVS_ERR_NOMEM, "defect-correction arrays");
+    void* p[6];
+    for (int k = 0; k < 6; k++)
+      if (!b->arena.alloc(p[k], k < 5 ? n4 : 4 * (size_t)b->nc)) return b->fail(FVS_ERR_NOMEM, "defect-correction arrays");
     b->dc.D = static_cast<float*>(p[0]); b->dc.D0 = static_cast<float*>(p[1]);
     b->dc.DF = static_cast<float*>(p[2]); b->dc.dP = static_cast<float*>(p[3]);
-    b->dc.R0 = static_cast<float*>(p[4]);
+    b->dc.R0 = static_cast<float*>(p[4]); b->dc.dtl = static_cast<float*>(p[5]);
   }
   cudaError_t e = cudaMemsetAsync(b->dc.D, 0, n4, b->stream);
   if (e == cudaSuccess) e = cudaMemsetAsync(b->dc.dP, 0, n4, b->stream);

@@ -215,6 +215,7 @@ struct DcView {
   float* DF = nullptr;   // stage accumulator (fcvar)
   float* dP = nullptr;   // primitive tangent of dU at the base state
   float* R0 = nullptr;   // FP64 residual of the base state, rounded to FP32
+  float* dtl = nullptr;  // [nc] local time step at the base state (FP32)
 };
 
 struct DcKernels {

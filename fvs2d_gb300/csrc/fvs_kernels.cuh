@@ -471,8 +471,16 @@ __device__ __forceinline__ void ghost_state(const DevView& d, int rec, double ti
 // ---------------------------------------------------------------------------
 // SPEC: non-strict builds only, kappa = 0 and no limiter (phi = 1), where the
 // reconstruction reduces to p + (dx, dy).grad exactly
-template <bool SPEC, bool COH>
+// REC: the reconstruction.  REC_GENERAL: UMUSCL with the limiter;
+// REC_SPEC (non-strict builds only): kappa = 0 and no limiter (phi = 1), where
+// the reconstruction reduces to p + (dx, dy).grad exactly; REC_FIRST: first
+// order, face states = cell states (the reference's p + 0 * (...) for finite
+// values) and no gradient is read.
+enum : int { REC_GENERAL = 0, REC_SPEC = 1, REC_FIRST = 2 };
+
+template <int REC, bool COH>
 __device__ __forceinline__ void flux_item(const DevView& d, int e, double time) {
+  constexpr bool SPEC = REC == REC_SPEC;
   const T* P = static_cast<const T*>(d.Pv);
   const T* GX = static_cast<const T*>(d.Gx);
   const T* GY = static_cast<const T*>(d.Gy);
@@ -480,9 +488,19 @@ __device__ __forceinline__ void flux_item(const DevView& d, int e, double time) 
   const int2 lr = d.ecell[e];
   const T2 n = ld2(d.enrm, e);
   const T af = static_cast<const T*>(d.earea)[e];
-  const T2 dl = ld2(d.edL, e);
   T pl[4], gxl[4], gyl[4], pfL[4], pfR[4];
   ldc4<COH>(P, lr.x, pl);
+  if (REC == REC_FIRST) {
+#pragma unroll
+    for (int v = 0; v < 4; v++) pfL[v] = pl[v];
+    if (lr.y >= 0) {
+      ldc4<COH>(P, lr.y, pfR);
+    } else {
+      const T2 xy = ld2(d.exy, e);
+      ghost_state(d, d.ebtype[e], time, xy.x, xy.y, n.x, n.y, pfL, pfR);
+    }
+  } else {
+  const T2 dl = ld2(d.edL, e);
   ldc4<COH>(GX, lr.x, gxl);
   ldc4<COH>(GY, lr.x, gyl);
   const T phiL = SPEC ? T(1) : ldc1<COH>(PH, lr.x);
@@ -519,6 +537,7 @@ __device__ __forceinline__ void flux_item(const DevView& d, int e, double time) 
     const T2 xy = ld2(d.exy, e);
     ghost_state(d, d.ebtype[e], time, xy.x, xy.y, n.x, n.y, pfL, pfR);
   }
+  }
   T flux[4], wsm;
 #if FVS_STRICT
   roe_flux(T(d.gamma), pfL, pfR, n.x, n.y, flux, wsm);
@@ -531,10 +550,10 @@ __device__ __forceinline__ void flux_item(const DevView& d, int e, double time) 
   static_cast<T*>(d.ews)[e] = wsm * af;
 }
 
-template <bool SPEC>
+template <int REC>
 __global__ void __launch_bounds__(256) k_flux(const DevView d, double dts) {
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
-  if (e < d.nedge) flux_item<SPEC, false>(d, e, d.tctl[1] + dts);
+  if (e < d.nedge) flux_item<REC, false>(d, e, d.tctl[1] + dts);
 }
 
 // ---------------------------------------------------------------------------
@@ -985,7 +1004,7 @@ __device__ __forceinline__ void update_tile(const DevView& d, const PersistPlan&
   }
 }
 
-template <int LIM, bool SPEC>
+template <int LIM, int REC>
 __global__ void __launch_bounds__(256) k_persistent(const DevView d, const PersistPlan p) {
   const int nb = gridDim.x;
   const int step0 = *p.step0_dev;
@@ -993,7 +1012,7 @@ __global__ void __launch_bounds__(256) k_persistent(const DevView d, const Persi
     const double told = p.t1 + double(step0 + s) * d.dt;
     for (int k = 0; k < p.nstages; k++) {
       const StageParams& sp = p.sp[k];
-      if (!d.first_order) {
+      if (REC != REC_FIRST) {
         for (int t = blockIdx.x; t < p.ncell_tiles; t += nb) {
           const int4 tl = p.cell_tiles[t];
           for (int ic = tl.x + threadIdx.x; ic < tl.y; ic += blockDim.x) gradient_item<FVS_GRAD_LSQ, LIM, true>(d, ic);
@@ -1002,7 +1021,7 @@ __global__ void __launch_bounds__(256) k_persistent(const DevView d, const Persi
       }
       for (int t = blockIdx.x; t < p.nedge_tiles; t += nb) {
         const int2 tl = p.edge_tiles[t];
-        for (int e = tl.x + threadIdx.x; e < tl.y; e += blockDim.x) flux_item<SPEC, true>(d, e, told + sp.dts);
+        for (int e = tl.x + threadIdx.x; e < tl.y; e += blockDim.x) flux_item<REC, true>(d, e, told + sp.dts);
       }
       if (!grid_sync(p.bar, p.budget)) return;
       for (int t = blockIdx.x; t < p.ncell_tiles; t += nb) {
@@ -1030,7 +1049,7 @@ __global__ void __launch_bounds__(256) k_persistent(const DevView d, const Persi
   }
 }
 
-template <int LIM, bool SPEC>
+template <int LIM, int REC>
 static cudaError_t launch_persistent_t(const DevView& d, const PersistPlan& p, int grid, int block, cudaStream_t s) {
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)grid);
@@ -1041,7 +1060,7 @@ static cudaError_t launch_persistent_t(const DevView& d, const PersistPlan& p, i
   attr[0].val.cooperative = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  return cudaLaunchKernelEx(&cfg, k_persistent<LIM, SPEC>, d, p);
+  return cudaLaunchKernelEx(&cfg, k_persistent<LIM, REC>, d, p);
 }
 
 static bool persistent_spec(const DevView& d) {
@@ -1052,16 +1071,19 @@ static int persistent_occupancy(const DevView& d, int block) {
   if (d.grad_method != FVS_GRAD_LSQ) return 0;
   int n = 0;
   cudaError_t e;
-  if (d.limiter != FVS_LIM_NONE) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_persistent<1, false>, block, 0);
-  else if (persistent_spec(d)) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_persistent<0, true>, block, 0);
-  else e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_persistent<0, false>, block, 0);
+  if (d.first_order) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_persistent<0, REC_FIRST>, block, 0);
+  else if (d.limiter != FVS_LIM_NONE)
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_persistent<1, REC_GENERAL>, block, 0);
+  else if (persistent_spec(d)) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_persistent<0, REC_SPEC>, block, 0);
+  else e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_persistent<0, REC_GENERAL>, block, 0);
   return e == cudaSuccess ? n : 0;
 }
 
 static cudaError_t launch_persistent(const DevView& d, const PersistPlan& p, int grid, int block, cudaStream_t s) {
-  if (d.limiter != FVS_LIM_NONE) return launch_persistent_t<1, false>(d, p, grid, block, s);
-  if (persistent_spec(d)) return launch_persistent_t<0, true>(d, p, grid, block, s);
-  return launch_persistent_t<0, false>(d, p, grid, block, s);
+  if (d.first_order) return launch_persistent_t<0, REC_FIRST>(d, p, grid, block, s);
+  if (d.limiter != FVS_LIM_NONE) return launch_persistent_t<1, REC_GENERAL>(d, p, grid, block, s);
+  if (persistent_spec(d)) return launch_persistent_t<0, REC_SPEC>(d, p, grid, block, s);
+  return launch_persistent_t<0, REC_GENERAL>(d, p, grid, block, s);
 }
 
 // ---------------------------------------------------------------------------
@@ -1088,8 +1110,9 @@ static void launch_gradient(const DevView& d, cudaStream_t s) {
 
 static void launch_flux(const DevView& d, double dts, cudaStream_t s) {
   const bool spec = !FVS_STRICT && d.khalf == 0.0 && d.omk == 1.0 && d.limiter == FVS_LIM_NONE && !d.first_order;
-  if (spec) k_flux<true><<<grid_of(d.nedge), 256, 0, s>>>(d, dts);
-  else k_flux<false><<<grid_of(d.nedge), 256, 0, s>>>(d, dts);
+  if (d.first_order) k_flux<REC_FIRST><<<grid_of(d.nedge), 256, 0, s>>>(d, dts);
+  else if (spec) k_flux<REC_SPEC><<<grid_of(d.nedge), 256, 0, s>>>(d, dts);
+  else k_flux<REC_GENERAL><<<grid_of(d.nedge), 256, 0, s>>>(d, dts);
 }
 
 static void launch_update(const DevView& d, const StageParams& sp, cudaStream_t s) {
@@ -1178,7 +1201,7 @@ __device__ __forceinline__ void dc_flux_item(const DevView& d, const DcView& c, 
 // |dU - dU0|^2 to d2.
 template <int MODE>
 __device__ __forceinline__ void dc_update_item(const DevView& d, const DcView& c, const StageParams& sp, int ic,
-                                               double* d2) {
+                                               float* d2) {
   float acc[4] = {0.f, 0.f, 0.f, 0.f};
   const int4 cf = d.cflist[ic];
   const int sl[4] = {cf.x, cf.y, cf.z, cf.w};
@@ -1196,7 +1219,7 @@ __device__ __forceinline__ void dc_update_item(const DevView& d, const DcView& c
   ld4(c.R0, ic, r0);
 #pragma unroll
   for (int v = 0; v < 4; v++) res[v] = r0[v] + acc[v] * rv;
-  const float h = float(d.dtl[ic] * sp.cst);
+  const float h = c.dtl[ic] * float(sp.cst);
   float u0[4], u[4], f[4];
   if (sp.stage == 1) {
     ldc4<true>(c.D, ic, u0);
@@ -1234,14 +1257,14 @@ __device__ __forceinline__ void dc_update_item(const DevView& d, const DcView& c
   if (sp.last) {
 #pragma unroll
     for (int v = 0; v < 4; v++) {
-      const double dd = double(u[v] - u0[v]);
+      const float dd = u[v] - u0[v];
       d2[v] += dd * dd;
     }
   }
 }
 
 template <int MODE>
-__global__ void __launch_bounds__(256) k_persistent_dc(const DevView d, const PersistPlan p, const DcView c) {
+__global__ void __launch_bounds__(256, 3) k_persistent_dc(const DevView d, const PersistPlan p, const DcView c) {
   const int nb = gridDim.x;
   const int step0 = *p.step0_dev;
   for (int s = 0; s < p.nsteps; s++) {
@@ -1254,9 +1277,10 @@ __global__ void __launch_bounds__(256) k_persistent_dc(const DevView d, const Pe
       if (!grid_sync(p.bar, p.budget)) return;
       for (int t = blockIdx.x; t < p.ncell_tiles; t += nb) {
         const int4 tl = p.cell_tiles[t];
-        double d2[4] = {0.0, 0.0, 0.0, 0.0};
-        for (int ic = tl.x + threadIdx.x; ic < tl.y; ic += blockDim.x) dc_update_item<MODE>(d, c, sp, ic, d2);
+        float d2f[4] = {0.f, 0.f, 0.f, 0.f};
+        for (int ic = tl.x + threadIdx.x; ic < tl.y; ic += blockDim.x) dc_update_item<MODE>(d, c, sp, ic, d2f);
         if (sp.last) {
+          const double d2[4] = {f2d_bits(d2f[0]), f2d_bits(d2f[1]), f2d_bits(d2f[2]), f2d_bits(d2f[3])};
           double out[4];
           block_sum4(d2, out);
           if (threadIdx.x == 0)
@@ -1312,6 +1336,7 @@ __global__ void __launch_bounds__(256) k_dc_base(const DevView d, const DcView c
   st4(c.R0, ic, rf);
   // compute_local_time, src/runge_kutta.f90:424-437, at the base state
   d.dtl[ic] = d.cfl * d.vol[ic] / (0.5 * ws64[ic]);
+  c.dtl[ic] = d2f_bits(d.dtl[ic]);
 }
 
 static void dc_fold(const DevView& d, const DcView& c, double* U64, cudaStream_t s) {
