@@ -78,12 +78,15 @@ def _split_quads(a, b, c, d, diag_ac):
 
 
 def periodic_square(nx: int, ny: int, x0: float = -5.0, y0: float = -5.0, lx: float = 10.0,
-                    ly: float = 10.0, seed: int = 1, jitter: float = 0.0, jitter_seed: int = 2) -> Mesh:
+                    ly: float = 10.0, seed: int = 1, jitter: float = 0.0, jitter_seed: int = 2,
+                    quad_every: int = 0) -> Mesh:
     """Doubly periodic box of nx*ny quads, 2*nx*ny triangles.
 
     Node (i,j) has id j*nx+i+1; the nodes at x0+lx / y0+ly are the ones at
     x0 / y0.  ``jitter`` displaces every node by a seeded uniform amount in
-    [-jitter*h, +jitter*h] per axis."""
+    [-jitter*h, +jitter*h] per axis.  ``quad_every`` > 0 keeps the quads of
+    every column i with i % quad_every == 0 (a mixed triangle/quad mesh;
+    cells are numbered triangles first, then quads)."""
     hx, hy = lx / nx, ly / ny
     i = np.arange(nx)
     j = np.arange(ny)
@@ -104,6 +107,11 @@ def periodic_square(nx: int, ny: int, x0: float = -5.0, y0: float = -5.0, lx: fl
     c = (jp * nx + ip + 1).astype(np.int32)
     d = (jp * nx + I + 1).astype(np.int32)
     diag = (splitmix64(seed, nx * ny) & np.uint64(1)).astype(bool)
+    if quad_every > 0:
+        keep = (I % quad_every) == 0
+        tris = _split_quads(a[~keep], b[~keep], c[~keep], d[~keep], diag[~keep])
+        quads = np.stack([a[keep], b[keep], c[keep], d[keep]], 1).astype(np.int32)
+        return Mesh(xy, tris, quads, [], [], lx, ly, f"periodic_mixed_{nx}x{ny}")
     tris = _split_quads(a, b, c, d, diag)
     return Mesh(xy, tris, np.zeros((0, 4), np.int32), [], [], lx, ly, f"periodic_{nx}x{ny}")
 
@@ -184,8 +192,9 @@ def _geometric_ratio(d1: np.ndarray, total: np.ndarray, n: int) -> np.ndarray:
 
 
 def naca0012_ogrid(nw: int = 512, nr: int = 256, first: float = 1.0e-3, far: float = 20.0,
-                   center=(0.5, 0.0), diag_ac: bool = True) -> Mesh:
-    """O-grid with nw wall nodes and nr radial nodes, 2*nw*(nr-1) triangles.
+                   center=(0.5, 0.0), diag_ac: bool = True, quads: bool = False) -> Mesh:
+    """O-grid with nw wall nodes and nr radial nodes, 2*nw*(nr-1) triangles
+    (``quads``: nw*(nr-1) quadrilaterals, like the reference's own example).
 
     Node (i,k) (i around the wall, k outward) has id k*nw+i+1."""
     s = 2.0 * math.pi * np.arange(nw) / nw
@@ -216,6 +225,14 @@ def naca0012_ogrid(nw: int = 512, nr: int = 256, first: float = 1.0e-3, far: flo
     b = ((qk + 1) * nw + qi + 1).astype(np.int32)
     c = ((qk + 1) * nw + ip + 1).astype(np.int32)
     d = (qk * nw + ip + 1).astype(np.int32)
+    if quads:
+        # cell q+1 is quad q = (qk, qi); wall cells k = 0, far cells k = nr-2,
+        # both in wall-node order
+        qq = np.stack([a, b, c, d], 1).astype(np.int32)
+        wall = (np.nonzero(qk == 0)[0] + 1).astype(np.int32)
+        farc = (np.nonzero(qk == nr - 2)[0] + 1).astype(np.int32)
+        return Mesh(xy, np.zeros((0, 3), np.int32), qq, ["slip_wall", "freestream"], [wall, farc], 0.0, 0.0,
+                    f"naca0012_quad_{nw}x{nr}")
     tris = _split_quads(a, b, c, d, np.full(a.shape[0], diag_ac))
     # wall cells: the triangle holding edge d-a (k=0); far cells: edge b-c (k=nr-2)
     ncell = tris.shape[0]

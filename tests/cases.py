@@ -36,6 +36,22 @@ def airfoil(nw=64, nr=24, **kw):
     return mesh, o.replace(**kw)
 
 
+def periodic_mixed(n=18, jitter=0.2, **kw):
+    """Periodic vortex on a mixed mesh: every third column of quads kept."""
+    mesh = meshgen.periodic_square(n, n, jitter=jitter, quad_every=3)
+    o = Options(**VORTEX, rk_nstages=3, rk_order=3, ssprk=True, cfl=0.8, dt_from_cfl=True)
+    return mesh, o.replace(**kw)
+
+
+def airfoil_quads(nw=64, nr=20, **kw):
+    """The transonic O-grid as quadrilaterals (like the reference's example
+    mesh), steady SSP-RK(4,2), LSQ-fn + Venkatakrishnan."""
+    mesh = meshgen.naca0012_ogrid(nw, nr, quads=True)
+    o = Options(mach_inf=0.8, aoa_inf_deg=1.25, steady=True, cfl=1.25, rk_nstages=4, rk_order=2, ssprk=True,
+                grad_method=3, lsq_stencil="fn", limiter=1, dt=0.01)
+    return mesh, o.replace(**kw)
+
+
 def mms_box(nx=16, ny=16, **kw):
     """Manufactured-solution box (ntstart=0, Dirichlet MMS boundary)."""
     mesh = meshgen.dirichlet_square(nx, ny, x0=0.0, y0=0.0, lx=1.0, ly=1.0, jitter=0.1)

@@ -54,6 +54,24 @@ def test_batch_equals_single_mesh_runs(prec):
         assert np.allclose(norms[c], ref_norms, rtol=1e-5 if prec == PREC_MIXED else 1e-12, atol=0)
 
 
+@pytest.mark.parametrize("first_order", [False, True])
+def test_batch_mixed_cell_types_strict(first_order):
+    """A quadrilateral O-grid and a triangular one in one batch, strict FP64:
+    each case bit-identical to its single-mesh run (second and first order)."""
+    kw = dict(reconst=1, limiter=0) if first_order else {}
+    m1, o1 = cases.airfoil_quads(40, 14, cfl=0.5, precision=PREC_FP64_STRICT, **kw)
+    m2, o2 = cases.airfoil(48, 16, cfl=0.5, mach_inf=0.6, aoa_inf_deg=2.0, precision=PREC_FP64_STRICT, **kw)
+    with Batch([m1, m2], [o1, o2]) as b:
+        b.initialize_solution()
+        b.steps(6)
+        got = [b.get_state(c) for c in range(2)]
+    for c, (m, o) in enumerate(((m1, o1), (m2, o2))):
+        with Solver(m, o) as s:
+            s.initialize_solution()
+            s.time_integration(0.0, 6)
+            assert np.array_equal(got[c], s.cvar), (c, rel(got[c], s.cvar))
+
+
 def test_batch_unsteady_periodic_strict():
     m1, o1 = cases.periodic_vortex(16, jitter=0.2, dt_from_cfl=False, dt=0.05, precision=PREC_FP64_STRICT)
     m2, o2 = cases.periodic_vortex(24, jitter=0.1, dt_from_cfl=False, dt=0.05, precision=PREC_FP64_STRICT)

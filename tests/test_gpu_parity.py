@@ -36,6 +36,11 @@ STRICT_RESIDUAL_CASES = {
     "airfoil_barth": lambda: cases.airfoil(limiter=2),
     "airfoil_albada": lambda: cases.airfoil(limiter=3),
     "airfoil_nn_nolim": lambda: cases.airfoil(lsq_stencil="nn", limiter=0),
+    "mixed_tri_quad_lsq_fn": lambda: cases.periodic_mixed(),
+    "mixed_tri_quad_ggcb": lambda: cases.periodic_mixed(grad_method=1),
+    "mixed_tri_quad_ggnb": lambda: cases.periodic_mixed(grad_method=2),
+    "quad_airfoil_venk": lambda: cases.airfoil_quads(),
+    "quad_airfoil_nn": lambda: cases.airfoil_quads(lsq_stencil="nn", limiter=0),
 }
 
 
@@ -95,6 +100,9 @@ INTEGRATOR_CASES = {
     "rk4_steady_airfoil": (lambda: cases.airfoil(ssprk=False, rk_order=4, cfl=0.8), 5, True),
     "ssprk42_dirichlet_vortex": (lambda: cases.dirichlet_vortex(ssprk=True, rk_order=2), 4, False),
     "rk4_dirichlet_vortex": (lambda: cases.dirichlet_vortex(), 4, False),
+    "ssprk3_mixed_tri_quad": (lambda: cases.periodic_mixed(14), 5, True),
+    "ssprk42_steady_quad_airfoil": (lambda: cases.airfoil_quads(48, 16), 5, True),
+    "ssprk42_steady_quad_airfoil_nn": (lambda: cases.airfoil_quads(48, 16, lsq_stencil="nn", limiter=0), 5, True),
 }
 
 

@@ -73,6 +73,8 @@ MESHES = {
     "dirichlet_jitter": lambda: meshgen.dirichlet_square(15, 9, jitter=0.2),
     "ogrid": lambda: meshgen.naca0012_ogrid(64, 24),
     "ogrid_bd": lambda: meshgen.naca0012_ogrid(40, 12, diag_ac=False),
+    "ogrid_quads": lambda: meshgen.naca0012_ogrid(48, 14, quads=True),
+    "periodic_mixed": lambda: meshgen.periodic_square(15, 12, jitter=0.2, quad_every=3),
 }
 OPTS = {
     "lsq_fn": Options(grad_method=3, lsq_stencil="fn"),

@@ -12,7 +12,7 @@ import math
 import numpy as np
 import pytest
 
-from cases import airfoil
+from cases import airfoil, airfoil_quads
 from oracle_lib import Oracle
 
 GAMMA = 1.4
@@ -92,10 +92,12 @@ def _perturbed(orc, seed):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("reconst,grad", [(2, 3), (1, 3), (2, 1), (2, 2)])
-def test_gpu_wall_loads_bit_exact(reconst, grad):
+@pytest.mark.parametrize("reconst,grad,quads", [(2, 3, False), (1, 3, False), (2, 1, False), (2, 2, False),
+                                                (2, 3, True), (2, 2, True)])
+def test_gpu_wall_loads_bit_exact(reconst, grad, quads):
     from fvs2d_gb300 import PREC_FP64_STRICT, Solver
-    mesh, o = airfoil(nw=64, nr=20, reconst=reconst, grad_method=grad, limiter=1 if grad == 3 else 0,
+    factory = airfoil_quads if quads else airfoil
+    mesh, o = factory(nw=64, nr=20, reconst=reconst, grad_method=grad, limiter=1 if grad == 3 else 0,
                       precision=PREC_FP64_STRICT)
     orc = Oracle(mesh, o)
     orc.initialize_solution()
