@@ -139,9 +139,11 @@ def run_airfoil(nw=512, nr=256, mach=0.8, aoa=1.25, drop=1e-10, switch=1e-5, max
 
 def profile_batch(ncases=16, steps=400, chunk=200):
     """A fixed amount of batched work for kernel profiling: the 16-case reduced
-    sweep (261,780 cells), `steps` mixed persistent steps, then `steps`
-    defect-correction steps, in chunks of `chunk` (one cooperative launch
-    each).  Returns the per-phase seconds."""
+    sweep (261,780 cells), the launch shape the autotuner picks for it (256
+    threads, tiles of 1024, 2 blocks per SM), `steps` mixed persistent steps,
+    then `steps` defect-correction steps, in chunks of `chunk`: one
+    cooperative launch each, steps / chunk launches per phase.  Returns the
+    per-phase seconds."""
     from .batch import Batch
     cases = sweep.draw_cases(ncases, 6, (64, 192), (32, 96))
     meshes = [c.mesh() for c in cases]
@@ -149,6 +151,8 @@ def profile_batch(ncases=16, steps=400, chunk=200):
     out = {"cells": int(sum(m.ncells for m in meshes)), "steps": steps, "chunk": chunk}
     with Batch(meshes, [sweep.case_options(c, PREC_MIXED) for c in cases]) as b:
         b.initialize_solution()
+        b.set_launch(256, 1024, 2)
+        out["launch"] = {k: v for k, v in b.info().items() if k in ("block", "tile", "blocks_per_sm", "graph")}
         t0 = time.perf_counter()
         b.run_to_level(steps, never, chunk)
         t1 = time.perf_counter()
