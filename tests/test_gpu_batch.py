@@ -92,10 +92,12 @@ def test_batch_unsteady_periodic_strict():
             assert np.array_equal(g, s.cvar)
 
 
-def test_barrier_timeout_reported_and_recoverable():
-    """A zero wait budget makes every grid-barrier wait run out: the kernel
-    returns, the call reports FVS_ERR_TIMEOUT, and the batch still works."""
-    meshes, opts = sweep(2)
+@pytest.mark.parametrize("first_order", [False, True])
+def test_barrier_timeout_reported_and_recoverable(first_order):
+    """A zero wait budget makes every grid-barrier wait run out (second- and
+    first-order persistent kernels): the kernel returns, the call reports
+    FVS_ERR_TIMEOUT, and the batch still works."""
+    meshes, opts = sweep(2, **(dict(reconst=1, limiter=0) if first_order else {}))
     with Batch(meshes, opts) as b:
         b.initialize_solution()
         b.set_barrier_budget(0.0)
