@@ -365,16 +365,22 @@ def main():
     ap.add_argument("--no-variants", dest="variants", action="store_false")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=12.0)
-    ap.add_argument("--workload", default="vortex", choices=["vortex", "sweep", "airfoil"],
+    ap.add_argument("--workload", default="vortex", choices=["vortex", "sweep", "airfoil", "vortex-period"],
                     help="vortex: the 1,048,576-cell throughput case (default); sweep: time to a 1e-10 drop on an "
                          "airfoil sweep, plain FP64 vs batched ladder vs learned warm start; airfoil: time to a "
-                         "1e-10 drop on the 261,120-cell NACA0012 O-grid, plain FP64 vs the ladder")
+                         "1e-10 drop on the 261,120-cell NACA0012 O-grid, plain FP64 vs the ladder; vortex-period: "
+                         "errors of the arithmetic modes after one vortex period at 1,048,576 cells")
     ap.add_argument("--n-train", type=int, default=96)
     ap.add_argument("--n-test", type=int, default=24)
     ap.add_argument("--full-size", action="store_true",
                     help="sweep meshes from the full distribution (64-512 wall x 32-256 radial nodes) instead of "
                          "64-192 x 32-96")
     args = ap.parse_args()
+    if args.workload == "vortex-period":
+        from fvs2d_gb300 import _build, accuracy
+        _build.build()
+        print(json.dumps(accuracy.run()), flush=True)
+        return
     if args.workload in ("sweep", "airfoil"):
         from fvs2d_gb300 import _build, sweep_bench
         _build.build()

@@ -150,6 +150,13 @@ class Solver:
         raw = names.raw
         return [(raw[32 * i:32 * i + 32].split(b"\0")[0].decode(), ms[i]) for i in range(n.value)]
 
+    def current_dt(self) -> float:
+        """The global dt in use (derived from the CFL at the first step when
+        dt_from_cfl is set)."""
+        s = capi.FvsSizes()
+        self._check(self._lib.fvs_get_sizes(self._h, C.byref(s)))
+        return float(s.dt)
+
     def launches_per_step(self) -> int:
         n = C.c_int32(0)
         self._check(self._lib.fvs_launches_per_step(self._h, C.byref(n)))
