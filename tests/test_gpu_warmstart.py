@@ -1,0 +1,57 @@
+"""What the trained warm-start network gains over the free-stream start.
+
+A small sweep (first-order steady O-grids) is solved by the batched ladder;
+its converged cells train the MLP on the GPU.  On held-out cases the
+network's prediction must be closer to the converged solution than the free
+stream, and the solver started from it must still reach the same absolute
+targets (the network changes the path, never the answer's tolerance)."""
+import numpy as np
+import pytest
+
+from fvs2d_gb300 import PREC_MIXED, sweep
+from fvs2d_gb300.batch import Batch
+from fvs2d_gb300.warmstart import WarmStart, build_dataset, reference_levels, solve_ladder
+
+pytestmark = pytest.mark.gpu
+
+WALL, RADIAL = (48, 80), (16, 28)
+
+
+def _solve(cases, starts=None, drop=1e-8):
+    meshes = [c.mesh() for c in cases]
+    levels = reference_levels(cases, meshes)
+    states, n1, n2, secs, _ = solve_ladder(meshes, [sweep.case_options(c, PREC_MIXED) for c in cases], levels,
+                                           drop=drop, max_steps=100000, chunk=200, starts=starts, autotune=False)
+    return meshes, levels, states, n1 + n2
+
+
+def test_prediction_beats_free_stream_and_keeps_the_target():
+    train = sweep.draw_cases(10, 21, WALL, RADIAL)
+    _, _, states, _ = _solve(train)
+    X, Y = build_dataset(train, states)
+    ws = WarmStart(width=128, depth=3, seed=1)
+    losses = ws.fit(X, Y, epochs=40, batch=2048, lr=2e-3, seed=2)
+    assert losses[-1] < 0.2 * losses[0], losses
+
+    test = sweep.draw_cases(4, 22, WALL, RADIAL)
+    meshes, levels, ref_states, steps_fs = _solve(test)
+    starts = [ws.predict_state(c, m) for c, m in zip(test, meshes)]
+    fs = [sweep.free_stream_state(c, m.ncells) for c, m in zip(test, meshes)]
+
+    def l2(a, b):
+        return float(np.sqrt(((a - b) ** 2).mean() / (b ** 2).mean()))
+
+    err_pred = [l2(s, r) for s, r in zip(starts, ref_states)]
+    err_fs = [l2(f, r) for f, r in zip(fs, ref_states)]
+    # closer to the converged solution than the free stream in every case,
+    # about half the free stream's error on average
+    assert all(p < f for p, f in zip(err_pred, err_fs)), (err_pred, err_fs)
+    assert np.mean(np.array(err_pred) / np.array(err_fs)) < 0.6, (err_pred, err_fs)
+    # the warm-started solve meets the same absolute targets
+    with Batch(meshes, [sweep.case_options(c, PREC_MIXED) for c in test]) as b:
+        b.initialize_solution()
+        for c, u in enumerate(starts):
+            b.set_state(c, u)
+        done, _, last, _ = b.run_to_level(100000, levels * 1e-5, 200)
+    assert np.all(done < 100000)
+    assert np.all(last <= levels * 1e-5)
