@@ -56,7 +56,7 @@ class Batch:
         launch = (C.c_int32 * 4)()
         self._check(self._lib.fvs_batch_info(self._h, C.byref(nc), C.byref(ne), launch))
         return {"ncells": nc.value, "nedges": ne.value, "block": launch[0], "tile": launch[1],
-                "blocks_per_sm": launch[2], "graph": bool(launch[3])}
+                "blocks_per_sm": launch[2], "graph": bool(launch[3] & 1), "tiled": bool(launch[3] & 2)}
 
     def initialize_solution(self):
         self._check(self._lib.fvs_batch_init_state(self._h))
@@ -101,6 +101,11 @@ class Batch:
         self._check(self._lib.fvs_batch_run_to_drop(self._h, int(max_steps), float(drop), int(chunk), capi.ptr(done),
                                                     capi.ptr(first), capi.ptr(last), C.byref(ms)))
         return done, first, last, ms.value
+
+    def set_mode(self, tiled: bool) -> None:
+        """Launch mode: a persistent cooperative kernel per chunk (False) or a
+        graph of per-phase tile launches per step (True)."""
+        self._check(self._lib.fvs_batch_set_mode(self._h, 1 if tiled else 0))
 
     def set_groups(self, group=None) -> None:
         """Cases with the same group id stop together when the first of them

@@ -101,6 +101,7 @@ SIGNATURES = {
     "fvs_batch_steps": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.POINTER(C.c_float)]),
     "fvs_batch_run_to_drop": (C.c_int, [C.c_void_p, C.c_int32, C.c_double, C.c_int32, C.c_void_p, C.c_void_p,
                                         C.c_void_p, C.POINTER(C.c_float)]),
+    "fvs_batch_set_mode": (C.c_int, [C.c_void_p, C.c_int32]),
     "fvs_batch_set_groups": (C.c_int, [C.c_void_p, C.c_void_p]),
     "fvs_batch_run_to_level": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p,
                                          C.c_void_p, C.POINTER(C.c_float)]),

@@ -77,6 +77,7 @@ struct fvs_batch {
     bool built = false;
     DevView d;
     int block = 256, tile = 1024, bps = 1;
+    bool tiled = false;
   } var[4];
   int nc = 0, ne = 0;
   std::vector<int> coff, eoff, cnum, enumv;  // per-case cell / edge-slot ranges
@@ -106,10 +107,17 @@ struct fvs_batch {
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   int* h_step0 = nullptr;
   DcView dc;  // defect-correction arrays, allocated on first use
+  // launch mode: false = one cooperative persistent launch per chunk, true =
+  // a CUDA graph of one step's tile launches, replayed once per step
+  bool tiled = false;
+  cudaGraphExec_t tgraph = nullptr;     // one step, current plan and precision
+  cudaGraphExec_t tgraph_dc = nullptr;  // one defect-correction step
   std::vector<int> group;  // cases of one group stop together (first to converge)
 
   ~fvs_batch() {
     if (graph) cudaGraphExecDestroy(graph);
+    if (tgraph) cudaGraphExecDestroy(tgraph);
+    if (tgraph_dc) cudaGraphExecDestroy(tgraph_dc);
     if (ev0) cudaEventDestroy(ev0);
     if (ev1) cudaEventDestroy(ev1);
     if (h_step0) cudaFreeHost(h_step0);
@@ -228,6 +236,30 @@ void set_batch_stages(fvs_batch* B) {
   B->d.dt = o.dt;
 }
 
+void drop_tiled_graphs(fvs_batch* B) {
+  if (B->tgraph) cudaGraphExecDestroy(B->tgraph);
+  if (B->tgraph_dc) cudaGraphExecDestroy(B->tgraph_dc);
+  B->tgraph = B->tgraph_dc = nullptr;
+}
+
+// a graph of whatever `enqueue` launches on the batch's stream
+template <typename F>
+cudaError_t capture_graph(fvs_batch* B, cudaGraphExec_t* out, F enqueue) {
+  cudaGraph_t g;
+  cudaError_t e = cudaStreamBeginCapture(B->stream, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) return e;
+  cudaError_t le = enqueue();
+  e = cudaStreamEndCapture(B->stream, &g);
+  if (e != cudaSuccess) return e;
+  if (le != cudaSuccess) {
+    cudaGraphDestroy(g);
+    return le;
+  }
+  e = cudaGraphInstantiate(out, g, 0);
+  cudaGraphDestroy(g);
+  return e;
+}
+
 // tile lists of the active cases for the current tile length
 int build_plan(fvs_batch* B) {
   std::vector<int4> ct, cases;
@@ -283,6 +315,7 @@ int build_plan(fvs_batch* B) {
     cudaGraphExecDestroy(B->graph);
     B->graph = nullptr;
   }
+  drop_tiled_graphs(B);
   B->graph_steps = -1;
   B->plan_dirty = false;
   return FVS_OK;
@@ -303,6 +336,17 @@ int launch_chunk(fvs_batch* B, int nsteps, int step0) {
   *B->h_step0 = step0;
   cudaError_t e = cudaMemcpyAsync(B->d_step0, B->h_step0, sizeof(int), cudaMemcpyHostToDevice, B->stream);
   if (e != cudaSuccess) return B->cuda_fail(e, "step upload");
+  if (B->tiled) {
+    // the step counter on the device advances at the end of each step
+    B->plan.nsteps = 1;
+    if (!B->tgraph) {
+      e = capture_graph(B, &B->tgraph, [&]() { return B->ks->tiled_step(B->d, B->plan, B->block, B->stream); });
+      if (e != cudaSuccess) return B->cuda_fail(e, "tiled step capture");
+    }
+    e = cudaMemsetAsync(B->d_bar, 0, sizeof(GridBarrier), B->stream);
+    for (int i = 0; i < nsteps && e == cudaSuccess; i++) e = cudaGraphLaunch(B->tgraph, B->stream);
+    return e == cudaSuccess ? FVS_OK : B->cuda_fail(e, "tiled step launch");
+  }
   const int grid = grid_size(B);
   B->plan.nsteps = nsteps;
   if (B->use_graph && B->graph_steps != nsteps) {
@@ -466,7 +510,7 @@ int fvs_batch_info(const fvs_batch* b, int32_t* ncells, int32_t* nedges, int32_t
     launch4[0] = b->block;
     launch4[1] = b->tile;
     launch4[2] = b->bps;
-    launch4[3] = b->use_graph ? 1 : 0;
+    launch4[3] = (b->use_graph ? 1 : 0) | (b->tiled ? 2 : 0);
   }
   return FVS_OK;
 }
@@ -518,7 +562,7 @@ int fvs_batch_set_precision(fvs_batch* b, int32_t precision) {
   fvs_batch::Variant& cur = b->var[b->prec];
   cur.built = true;
   cur.d = b->d;
-  cur.block = b->block; cur.tile = b->tile; cur.bps = b->bps;
+  cur.block = b->block; cur.tile = b->tile; cur.bps = b->bps; cur.tiled = b->tiled;
   fvs_batch::Variant& nxt = b->var[precision];
   const int old_prec = b->prec;
   b->prec = precision;
@@ -530,16 +574,17 @@ int fvs_batch_set_precision(fvs_batch* b, int32_t precision) {
       return rc;
     }
     nxt.built = true;
-    nxt.block = b->block; nxt.tile = b->tile; nxt.bps = b->bps;
+    nxt.block = b->block; nxt.tile = b->tile; nxt.bps = b->bps; nxt.tiled = b->tiled;
   }
   cudaError_t e = cudaMemcpyAsync(nxt.d.U, cur.d.U, 32 * (size_t)b->nc, cudaMemcpyDeviceToDevice, b->stream);
   if (e != cudaSuccess) return b->cuda_fail(e, "state copy");
   b->d = nxt.d;
   b->ks = kernels_for(precision);
   b->mixed = precision == FVS_PREC_MIXED;
-  b->block = nxt.block; b->tile = nxt.tile; b->bps = nxt.bps;
+  b->block = nxt.block; b->tile = nxt.tile; b->bps = nxt.bps; b->tiled = nxt.tiled;
   b->ks->cvar2pvar(b->d, b->stream);
   if (b->graph) { cudaGraphExecDestroy(b->graph); b->graph = nullptr; }
+  drop_tiled_graphs(b);
   b->graph_steps = -1;
   b->plan_dirty = true;
   e = cudaStreamSynchronize(b->stream);
@@ -553,6 +598,13 @@ int fvs_batch_set_groups(fvs_batch* b, const int32_t* group) {
     return FVS_OK;
   }
   b->group.assign(group, group + b->ncases);
+  return FVS_OK;
+}
+
+int fvs_batch_set_mode(fvs_batch* b, int32_t tiled) {
+  if (!b || tiled < 0 || tiled > 1) return FVS_ERR_INVALID;
+  b->tiled = tiled != 0;
+  b->plan_dirty = true;
   return FVS_OK;
 }
 
@@ -601,6 +653,8 @@ int fvs_batch_autotune(fvs_batch* b, int32_t trial_steps, float* best_ms) {
   const int tiles_per_block[3] = {1, 4, 16};
   float best = 1e30f;
   int bb = b->block, bt = b->tile, bp = b->bps;
+  bool btiled = b->tiled;
+  for (int mode = 0; mode < 2; mode++)
   for (int blk : blocks) {
     const int occ = b->ks->persistent_occupancy(b->d, blk);
     if (occ <= 0) continue;
@@ -608,9 +662,11 @@ int fvs_batch_autotune(fvs_batch* b, int32_t trial_steps, float* best_ms) {
     for (int tpb : tiles_per_block)
       for (int q = 0; q < 3; q++) {
         if (q > 0 && bps_list[q] == bps_list[q - 1]) continue;
+        if (mode == 1 && q > 0) continue;  // blocks per SM do not apply to tile launches
         b->block = blk;
         b->tile = blk * tpb;
         b->bps = bps_list[q];
+        b->tiled = mode == 1;
         b->plan_dirty = true;
         float ms = 0.f;
         int rc = fvs_batch_steps(b, 1, nullptr, nullptr);  // warm-up, graph capture
@@ -618,13 +674,14 @@ int fvs_batch_autotune(fvs_batch* b, int32_t trial_steps, float* best_ms) {
         if (rc) return rc;
         if (ms < best) {
           best = ms;
-          bb = blk; bt = blk * tpb; bp = bps_list[q];
+          bb = blk; bt = blk * tpb; bp = bps_list[q]; btiled = b->tiled;
         }
       }
   }
   b->block = bb;
   b->tile = bt;
   b->bps = bp;
+  b->tiled = btiled;
   b->plan_dirty = true;
   e = cudaMemcpy(b->d.U, b->d_backup, 32 * (size_t)b->nc, cudaMemcpyDeviceToDevice);
   if (e != cudaSuccess) return b->cuda_fail(e, "state restore");
@@ -745,7 +802,8 @@ int fvs_batch_run_to_level_dc(fvs_batch* b, int32_t max_steps, const double* lev
   // launch shape of the mixed variant (tuned there when the batch ran mixed)
   const fvs_batch::Variant& vm = b->var[FVS_PREC_MIXED];
   const int sb = b->block, st = b->tile, sp = b->bps;
-  if (vm.built) { b->block = vm.block; b->tile = vm.tile; b->bps = vm.bps; }
+  const bool stl = b->tiled;
+  if (vm.built) { b->block = vm.block; b->tile = vm.tile; b->bps = vm.bps; b->tiled = vm.tiled; }
   const int occ = K.occupancy(b->block);
   if (occ <= 0) return b->fail(FVS_ERR_INVALID, "no resident block for the defect-correction kernel");
   const int grid = std::max(1, std::min(b->bps, occ)) * b->nsm;
@@ -771,8 +829,15 @@ int fvs_batch_run_to_level_dc(fvs_batch* b, int32_t max_steps, const double* lev
     *b->h_step0 = step;
     e = cudaMemcpyAsync(b->d_step0, b->h_step0, sizeof(int), cudaMemcpyHostToDevice, b->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(b->d_bar, 0, sizeof(GridBarrier), b->stream);
-    b->plan.nsteps = n;
-    if (e == cudaSuccess) e = K.persistent(*d32, b->plan, b->dc, grid, b->block, b->stream);
+    if (b->tiled) {
+      b->plan.nsteps = 1;
+      if (e == cudaSuccess && !b->tgraph_dc)
+        e = capture_graph(b, &b->tgraph_dc, [&]() { return K.tiled_step(*d32, b->plan, b->dc, b->block, b->stream); });
+      for (int i = 0; i < n && e == cudaSuccess; i++) e = cudaGraphLaunch(b->tgraph_dc, b->stream);
+    } else {
+      b->plan.nsteps = n;
+      if (e == cudaSuccess) e = K.persistent(*d32, b->plan, b->dc, grid, b->block, b->stream);
+    }
     if (e != cudaSuccess) { rc = b->cuda_fail(e, "defect-correction chunk"); break; }
     if ((rc = check_barrier(b))) break;
     e = cudaMemcpy(all.data(), b->d_case_norms, 8 * all.size(), cudaMemcpyDeviceToHost);
@@ -813,7 +878,7 @@ int fvs_batch_run_to_level_dc(fvs_batch* b, int32_t max_steps, const double* lev
   e = cudaEventSynchronize(b->ev1);
   if (!rc && e != cudaSuccess) rc = b->cuda_fail(e, "defect-correction run");
   if (ms) cudaEventElapsedTime(ms, b->ev0, b->ev1);
-  b->block = sb; b->tile = st; b->bps = sp;
+  b->block = sb; b->tile = st; b->bps = sp; b->tiled = stl;
   std::fill(b->active.begin(), b->active.end(), 1);
   b->plan_dirty = true;
   if (steps_done) std::memcpy(steps_done, done.data(), 4 * (size_t)nc);

@@ -203,6 +203,8 @@ struct KernelSet {
   // size (0: the scheme has no persistent variant), and the cooperative launch
   int (*persistent_occupancy)(const DevView&, int block);
   cudaError_t (*persistent)(const DevView&, const PersistPlan&, int grid, int block, cudaStream_t);
+  // one step of the same tile work as separate launches (for graph capture)
+  cudaError_t (*tiled_step)(const DevView&, const PersistPlan&, int block, cudaStream_t);
 };
 // Defect correction of a first-order steady batch (mixed build): per chunk
 // the FP64 residual R0 of the base state is evaluated once; the RK stages
@@ -228,6 +230,7 @@ struct DcKernels {
   int (*occupancy)(int block);
   cudaError_t (*persistent)(const DevView& d32, const PersistPlan& p, const DcView& c, int grid, int block,
                             cudaStream_t);
+  cudaError_t (*tiled_step)(const DevView& d32, const PersistPlan& p, const DcView& c, int block, cudaStream_t);
 };
 const DcKernels& dc_kernels();
 

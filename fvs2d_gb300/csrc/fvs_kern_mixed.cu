@@ -10,11 +10,12 @@ namespace fvs {
 const KernelSet& kernels_mixed() {
   static const KernelSet k = {"mixed", k_mixed::launch_begin_step, k_mixed::launch_cvar2pvar, k_mixed::launch_gradient,
                               k_mixed::launch_flux, k_mixed::launch_update, k_mixed::launch_residual_out, k_mixed::persistent_occupancy,
-                              k_mixed::launch_persistent};
+                              k_mixed::launch_persistent, k_mixed::launch_tiled_step};
   return k;
 }
 const DcKernels& dc_kernels() {
-  static const DcKernels k = {k_mixed::dc_fold, k_mixed::dc_base, k_mixed::dc_occupancy, k_mixed::dc_persistent};
+  static const DcKernels k = {k_mixed::dc_fold, k_mixed::dc_base, k_mixed::dc_occupancy, k_mixed::dc_persistent,
+                              k_mixed::dc_tiled_step};
   return k;
 }
 }  // namespace fvs

@@ -1087,6 +1087,72 @@ static cudaError_t launch_persistent(const DevView& d, const PersistPlan& p, int
 }
 
 // ---------------------------------------------------------------------------
+// tiled step: the same tile work as the persistent kernel, one launch per
+// phase (one block per tile), for capture in a CUDA graph; the device step
+// counter (*step0_dev) advances at the end of each step
+// ---------------------------------------------------------------------------
+template <int LIM>
+__global__ void __launch_bounds__(256) k_tiles_gradient(const DevView d, const PersistPlan p) {
+  const int4 tl = p.cell_tiles[blockIdx.x];
+  for (int ic = tl.x + threadIdx.x; ic < tl.y; ic += blockDim.x) gradient_item<FVS_GRAD_LSQ, LIM, false>(d, ic);
+}
+
+template <int REC>
+__global__ void __launch_bounds__(256) k_tiles_flux(const DevView d, const PersistPlan p, int stage) {
+  const double told = p.t1 + double(*p.step0_dev) * d.dt;
+  const int2 tl = p.edge_tiles[blockIdx.x];
+  for (int e = tl.x + threadIdx.x; e < tl.y; e += blockDim.x) flux_item<REC, false>(d, e, told + p.sp[stage].dts);
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(256) k_tiles_update(const DevView d, const PersistPlan p, int stage) {
+  update_tile<MODE>(d, p, p.sp[stage], blockIdx.x);
+}
+
+// per-case RMS of the step from the tile partials (fixed order), one block
+// per active case; the last block to finish advances the step counter
+__global__ void __launch_bounds__(32) k_tiles_norms(const PersistPlan p) {
+  __shared__ int s_last;
+  const int step = *p.step0_dev;
+  if (threadIdx.x == 0) {
+    const int4 ct = p.case_tiles[blockIdx.x];
+    double a[4] = {0.0, 0.0, 0.0, 0.0};
+    for (int t = ct.y; t < ct.z; t++)
+#pragma unroll
+      for (int k = 0; k < 4; k++) a[k] += p.tile_partials[4 * (size_t)t + k];
+    double* o = p.case_norms + 4 * ((size_t)ct.x * p.norm_cap + step % p.norm_cap);
+#pragma unroll
+    for (int k = 0; k < 4; k++) o[k] = sqrt(a[k] / double(ct.w));
+    __threadfence();
+    s_last = atomicAdd(&p.bar->count, 1u) == gridDim.x - 1;
+    if (s_last) {
+      p.bar->count = 0u;
+      *const_cast<int*>(p.step0_dev) = step + 1;
+    }
+  }
+}
+
+static cudaError_t launch_tiled_step(const DevView& d, const PersistPlan& p, int block, cudaStream_t s) {
+  for (int k = 0; k < p.nstages; k++) {
+    if (!d.first_order) {
+      if (d.limiter != FVS_LIM_NONE) k_tiles_gradient<1><<<p.ncell_tiles, block, 0, s>>>(d, p);
+      else k_tiles_gradient<0><<<p.ncell_tiles, block, 0, s>>>(d, p);
+    }
+    if (d.first_order) k_tiles_flux<REC_FIRST><<<p.nedge_tiles, block, 0, s>>>(d, p, k);
+    else if (persistent_spec(d)) k_tiles_flux<REC_SPEC><<<p.nedge_tiles, block, 0, s>>>(d, p, k);
+    else k_tiles_flux<REC_GENERAL><<<p.nedge_tiles, block, 0, s>>>(d, p, k);
+    switch (p.sp[k].mode) {
+      case MODE_SSP42: k_tiles_update<MODE_SSP42><<<p.ncell_tiles, block, 0, s>>>(d, p, k); break;
+      case MODE_SSP3: k_tiles_update<MODE_SSP3><<<p.ncell_tiles, block, 0, s>>>(d, p, k); break;
+      default: k_tiles_update<MODE_RK><<<p.ncell_tiles, block, 0, s>>>(d, p, k); break;
+    }
+  }
+  k_tiles_norms<<<p.ncase_active, 32, 0, s>>>(p);
+  return cudaGetLastError();
+}
+
+
+// ---------------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------------
 static inline unsigned grid_of(int n) { return (unsigned)((n + 255) / 256); }
@@ -1364,6 +1430,39 @@ static cudaError_t dc_persistent(const DevView& d, const PersistPlan& p, const D
   cfg.numAttrs = 1;
   if (p.sp[0].mode == MODE_SSP42) return cudaLaunchKernelEx(&cfg, k_persistent_dc<MODE_SSP42>, d, p, c);
   return cudaLaunchKernelEx(&cfg, k_persistent_dc<MODE_RK>, d, p, c);
+}
+// one defect-correction step as tile launches (for graph capture)
+__global__ void __launch_bounds__(256) k_tiles_dc_flux(const DevView d, const DcView c, const PersistPlan p) {
+  const int2 tl = p.edge_tiles[blockIdx.x];
+  for (int e = tl.x + threadIdx.x; e < tl.y; e += blockDim.x) dc_flux_item(d, c, e);
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(256) k_tiles_dc_update(const DevView d, const DcView c, const PersistPlan p,
+                                                         int stage) {
+  const StageParams& sp = p.sp[stage];
+  const int t = blockIdx.x;
+  const int4 tl = p.cell_tiles[t];
+  float d2f[4] = {0.f, 0.f, 0.f, 0.f};
+  for (int ic = tl.x + threadIdx.x; ic < tl.y; ic += blockDim.x) dc_update_item<MODE>(d, c, sp, ic, d2f);
+  if (sp.last) {
+    const double d2[4] = {f2d_bits(d2f[0]), f2d_bits(d2f[1]), f2d_bits(d2f[2]), f2d_bits(d2f[3])};
+    double out[4];
+    block_sum4(d2, out);
+    if (threadIdx.x == 0)
+#pragma unroll
+      for (int q = 0; q < 4; q++) p.tile_partials[4 * (size_t)t + q] = out[q];
+  }
+}
+
+static cudaError_t dc_tiled_step(const DevView& d, const PersistPlan& p, const DcView& c, int block, cudaStream_t s) {
+  for (int k = 0; k < p.nstages; k++) {
+    k_tiles_dc_flux<<<p.nedge_tiles, block, 0, s>>>(d, c, p);
+    if (p.sp[k].mode == MODE_SSP42) k_tiles_dc_update<MODE_SSP42><<<p.ncell_tiles, block, 0, s>>>(d, c, p, k);
+    else k_tiles_dc_update<MODE_RK><<<p.ncell_tiles, block, 0, s>>>(d, c, p, k);
+  }
+  k_tiles_norms<<<p.ncase_active, 32, 0, s>>>(p);
+  return cudaGetLastError();
 }
 #endif  // FVS_MIXED
 

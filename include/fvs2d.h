@@ -239,7 +239,8 @@ int fvs_batch_create(const fvs_mesh* meshes, const fvs_options* opts, int32_t nc
                      fvs_batch** out);
 void fvs_batch_destroy(fvs_batch* b);
 const char* fvs_batch_last_error(const fvs_batch* b);
-/* total cells and edge slots; launch4 = {block, tile, blocks per SM, graph} */
+/* total cells and edge slots; launch4 = {block, tile, blocks per SM, flags}
+ * with flags bit 0 = persistent launches graph-captured, bit 1 = tiled mode */
 int fvs_batch_info(const fvs_batch* b, int32_t* ncells, int32_t* nedges, int32_t* launch4);
 int fvs_batch_init_state(fvs_batch* b);                                  /* free stream per case */
 int fvs_batch_set_state(fvs_batch* b, int32_t icase, const double* cvar); /* [ncells_case][4] */
@@ -247,6 +248,10 @@ int fvs_batch_get_state(fvs_batch* b, int32_t icase, double* cvar);
 /* times the launch-shape candidates on the batch (state restored after) */
 int fvs_batch_autotune(fvs_batch* b, int32_t trial_steps, float* best_ms_per_step);
 int fvs_batch_set_launch(fvs_batch* b, int32_t block, int32_t tile, int32_t blocks_per_sm);
+/* 0: one cooperative persistent launch per chunk of steps (grid barriers
+ * between phases); 1: each step a CUDA graph of tile launches, one block per
+ * tile and phase.  fvs_batch_autotune times both. */
+int fvs_batch_set_mode(fvs_batch* b, int32_t tiled);
 /* switches the arithmetic of all cases (FVS_PREC_*), keeping the FP64
  * state: e.g. MIXED until the FP32 flux floor, then FP64 to a 1e-10 drop */
 int fvs_batch_set_precision(fvs_batch* b, int32_t precision);

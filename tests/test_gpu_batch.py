@@ -110,6 +110,34 @@ def test_barrier_timeout_reported_and_recoverable(first_order):
         assert np.isfinite(norms).all()
 
 
+@pytest.mark.parametrize("prec,first_order", [(PREC_FP64_STRICT, False), (PREC_FP64_STRICT, True),
+                                               (PREC_MIXED, False)])
+def test_tiled_mode_equals_persistent(prec, first_order):
+    """A graph of per-phase tile launches runs the tile work of the persistent
+    kernel in the same order: strict FP64 states and norms bit-identical, over
+    two chunks (the device step counter restarts from the host's)."""
+    meshes, opts = sweep(prec=prec, **(dict(reconst=1, limiter=0) if first_order else {}))
+    res = []
+    for tiled in (False, True):
+        with Batch(meshes, opts) as b:
+            b.set_mode(tiled)
+            b.initialize_solution()
+            n1, _ = b.steps(5)
+            n2, _ = b.steps(3)
+            assert b.info()["tiled"] == tiled
+            res.append((np.concatenate([n1, n2], axis=1), [b.get_state(c) for c in range(len(meshes))]))
+    (np_, up), (nt, ut) = res
+    for c in range(len(meshes)):
+        if prec == PREC_FP64_STRICT:
+            assert np.array_equal(ut[c], up[c]), (c, rel(ut[c], up[c]))
+        else:
+            assert rel(ut[c], up[c]) <= STATE_TOL[prec], (c, rel(ut[c], up[c]))
+    if prec == PREC_FP64_STRICT:
+        assert np.array_equal(nt, np_)
+    else:
+        assert np.allclose(nt, np_, rtol=1e-5, atol=0)
+
+
 def test_autotune_keeps_state_and_results():
     meshes, opts = sweep(3)
     with Batch(meshes, opts) as b:

@@ -49,6 +49,26 @@ def test_one_step_chunks_follow_the_fp64_trajectory():
         assert err <= 1e-3 * inc, (c, err, inc)
 
 
+def test_tiled_mode_equals_persistent():
+    """Defect correction as a graph of tile launches per step: same tile work
+    as the persistent kernel, same states to FP32-increment rounding."""
+    meshes, opts = first_order_sweep(PREC_MIXED)
+    out = []
+    for tiled in (False, True):
+        with Batch(meshes, opts) as b:
+            b.set_mode(tiled)
+            b.initialize_solution()
+            b.steps(200)
+            never = np.zeros((3, 4))
+            done, _, last, _ = b.run_to_level(60, never, chunk=25, dc=True)
+            assert np.all(done == 60)
+            out.append(([b.get_state(c) for c in range(3)], last))
+    for c in range(3):
+        a, t = out[0][0][c], out[1][0][c]
+        assert np.abs(a - t).max() <= 1e-12 * np.abs(a).max(), c
+    assert np.allclose(out[0][1], out[1][1], rtol=1e-6, atol=0)
+
+
 def test_converges_to_the_fp64_fixed_point():
     meshes, opts = first_order_sweep(PREC_MIXED)
     with Batch(meshes, opts) as b:
