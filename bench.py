@@ -376,19 +376,18 @@ def main():
                     help="sweep meshes from the full distribution (64-512 wall x 32-256 radial nodes) instead of "
                          "64-192 x 32-96")
     args = ap.parse_args()
-    if args.workload == "vortex-period":
-        from fvs2d_gb300 import _build, accuracy
+    if args.workload in ("sweep", "airfoil", "vortex-period"):
+        from fvs2d_gb300 import _build, accuracy, sweep_bench
         _build.build()
-        print(json.dumps(accuracy.run()), flush=True)
-        return
-    if args.workload in ("sweep", "airfoil"):
-        from fvs2d_gb300 import _build, sweep_bench
-        _build.build()
-        if args.workload == "sweep":
+        clk = Clocks(int(os.environ.get("LOCAL_RANK", "0")))
+        if args.workload == "vortex-period":
+            out = accuracy.run()
+        elif args.workload == "sweep":
             sizes = dict(wall=(64, 512), radial=(32, 256), race=False) if args.full_size else {}
             out = sweep_bench.run(args.n_train, args.n_test, **sizes)
         else:
             out = sweep_bench.run_airfoil()
+        out["clocks"] = clk.stop()
         print(json.dumps(out), flush=True)
         return
     if args.warmup < 3 and args.impl == "ours":

@@ -56,7 +56,8 @@ class Batch:
         launch = (C.c_int32 * 4)()
         self._check(self._lib.fvs_batch_info(self._h, C.byref(nc), C.byref(ne), launch))
         return {"ncells": nc.value, "nedges": ne.value, "block": launch[0], "tile": launch[1],
-                "blocks_per_sm": launch[2], "graph": bool(launch[3] & 1), "tiled": bool(launch[3] & 2)}
+                "blocks_per_sm": launch[2], "graph": bool(launch[3] & 1), "tiled": bool(launch[3] & 2),
+                "fused": bool(launch[3] & 4)}
 
     def initialize_solution(self):
         self._check(self._lib.fvs_batch_init_state(self._h))
@@ -102,10 +103,14 @@ class Batch:
                                                     capi.ptr(first), capi.ptr(last), C.byref(ms)))
         return done, first, last, ms.value
 
-    def set_mode(self, tiled: bool) -> None:
-        """Launch mode: a persistent cooperative kernel per chunk (False) or a
-        graph of per-phase tile launches per step (True)."""
-        self._check(self._lib.fvs_batch_set_mode(self._h, 1 if tiled else 0))
+    def set_mode(self, tiled: bool, fused: bool = True, dc_fused: bool = False) -> None:
+        """Launch mode: a persistent cooperative kernel per chunk (tiled False)
+        or a graph of per-phase tile launches per step (True).  fused: first-
+        order mixed stages evaluate the flux per cell in one phase per stage
+        (where the stage count is even); dc_fused: the same for the
+        defect-correction stages."""
+        mode = (1 if tiled else 0) | (0 if fused else 2) | (4 if dc_fused else 0)
+        self._check(self._lib.fvs_batch_set_mode(self._h, mode))
 
     def set_groups(self, group=None) -> None:
         """Cases with the same group id stop together when the first of them

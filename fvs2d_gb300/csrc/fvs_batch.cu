@@ -112,6 +112,12 @@ struct fvs_batch {
   bool tiled = false;
   cudaGraphExec_t tgraph = nullptr;     // one step, current plan and precision
   cudaGraphExec_t tgraph_dc = nullptr;  // one defect-correction step
+  // fused first-order stages (flux per cell, one phase per stage) where they
+  // apply, in the mixed phase (fuse) and in defect correction (fuse_dc);
+  // second buffers of the primitives and of the correction tangents
+  bool fuse = true, fuse_dc = false;
+  void* pv2_mem = nullptr;
+  void* dp2_mem = nullptr;
   std::vector<int> group;  // cases of one group stop together (first to converge)
 
   ~fvs_batch() {
@@ -260,8 +266,22 @@ cudaError_t capture_graph(fvs_batch* B, cudaGraphExec_t* out, F enqueue) {
   return e;
 }
 
+// The fused first-order stage: mixed precision, first order and an even
+// number of stages (each step then ends in the primary primitive buffer).
+bool fusable(const fvs_batch* B) { return B->base.reconst == FVS_RECON_UPWIND1 && B->stages.size() % 2 == 0; }
+
+int apply_fusion(fvs_batch* B) {
+  B->d.Pv2 = nullptr;
+  if (!(B->fuse && fusable(B) && B->prec == FVS_PREC_MIXED)) return FVS_OK;
+  if (!B->pv2_mem && !B->arena.alloc(B->pv2_mem, 16 * (size_t)B->nc))
+    return B->fail(FVS_ERR_NOMEM, "second primitive buffer");
+  B->d.Pv2 = B->pv2_mem;
+  return FVS_OK;
+}
+
 // tile lists of the active cases for the current tile length
 int build_plan(fvs_batch* B) {
+  if (int rc = apply_fusion(B)) return rc;
   std::vector<int4> ct, cases;
   std::vector<int2> et;
   for (int c = 0; c < B->ncases; c++) {
@@ -510,7 +530,7 @@ int fvs_batch_info(const fvs_batch* b, int32_t* ncells, int32_t* nedges, int32_t
     launch4[0] = b->block;
     launch4[1] = b->tile;
     launch4[2] = b->bps;
-    launch4[3] = (b->use_graph ? 1 : 0) | (b->tiled ? 2 : 0);
+    launch4[3] = (b->use_graph ? 1 : 0) | (b->tiled ? 2 : 0) | (b->d.Pv2 ? 4 : 0);
   }
   return FVS_OK;
 }
@@ -601,9 +621,11 @@ int fvs_batch_set_groups(fvs_batch* b, const int32_t* group) {
   return FVS_OK;
 }
 
-int fvs_batch_set_mode(fvs_batch* b, int32_t tiled) {
-  if (!b || tiled < 0 || tiled > 1) return FVS_ERR_INVALID;
-  b->tiled = tiled != 0;
+int fvs_batch_set_mode(fvs_batch* b, int32_t mode) {
+  if (!b || mode < 0 || mode > (FVS_BATCH_TILED | FVS_BATCH_UNFUSED | FVS_BATCH_DC_FUSED)) return FVS_ERR_INVALID;
+  b->tiled = (mode & FVS_BATCH_TILED) != 0;
+  b->fuse = (mode & FVS_BATCH_UNFUSED) == 0;
+  b->fuse_dc = (mode & FVS_BATCH_DC_FUSED) != 0;
   b->plan_dirty = true;
   return FVS_OK;
 }
@@ -653,9 +675,15 @@ int fvs_batch_autotune(fvs_batch* b, int32_t trial_steps, float* best_ms) {
   const int tiles_per_block[3] = {1, 4, 16};
   float best = 1e30f;
   int bb = b->block, bt = b->tile, bp = b->bps;
-  bool btiled = b->tiled;
+  bool btiled = b->tiled, bfuse = b->fuse;
+  // the fused first-order stage is timed against the separate phases where
+  // it applies
+  const int nfuse = (b->prec == FVS_PREC_MIXED && fusable(b)) ? 2 : 1;
+  for (int fz = 0; fz < nfuse; fz++)
   for (int mode = 0; mode < 2; mode++)
   for (int blk : blocks) {
+    if (nfuse == 2) b->fuse = fz == 1;
+    if (int rc = apply_fusion(b)) return rc;  // the occupancy below is the variant's
     const int occ = b->ks->persistent_occupancy(b->d, blk);
     if (occ <= 0) continue;
     const int bps_list[3] = {1, std::max(1, occ / 2), occ};
@@ -674,7 +702,7 @@ int fvs_batch_autotune(fvs_batch* b, int32_t trial_steps, float* best_ms) {
         if (rc) return rc;
         if (ms < best) {
           best = ms;
-          bb = blk; bt = blk * tpb; bp = bps_list[q]; btiled = b->tiled;
+          bb = blk; bt = blk * tpb; bp = bps_list[q]; btiled = b->tiled; bfuse = b->fuse;
         }
       }
   }
@@ -682,6 +710,7 @@ int fvs_batch_autotune(fvs_batch* b, int32_t trial_steps, float* best_ms) {
   b->tile = bt;
   b->bps = bp;
   b->tiled = btiled;
+  b->fuse = bfuse;
   b->plan_dirty = true;
   e = cudaMemcpy(b->d.U, b->d_backup, 32 * (size_t)b->nc, cudaMemcpyDeviceToDevice);
   if (e != cudaSuccess) return b->cuda_fail(e, "state restore");
@@ -804,7 +833,11 @@ int fvs_batch_run_to_level_dc(fvs_batch* b, int32_t max_steps, const double* lev
   const int sb = b->block, st = b->tile, sp = b->bps;
   const bool stl = b->tiled;
   if (vm.built) { b->block = vm.block; b->tile = vm.tile; b->bps = vm.bps; b->tiled = vm.tiled; }
-  const int occ = K.occupancy(b->block);
+  const bool fuse_dc = b->fuse_dc && fusable(b);
+  if (fuse_dc && !b->dp2_mem && !b->arena.alloc(b->dp2_mem, 16 * (size_t)b->nc))
+    return b->fail(FVS_ERR_NOMEM, "second tangent buffer");
+  b->dc.dP2 = fuse_dc ? static_cast<float*>(b->dp2_mem) : nullptr;
+  const int occ = K.occupancy(b->dc, b->block);
   if (occ <= 0) return b->fail(FVS_ERR_INVALID, "no resident block for the defect-correction kernel");
   const int grid = std::max(1, std::min(b->bps, occ)) * b->nsm;
   const int nc = b->ncases;

@@ -83,6 +83,8 @@ struct DevView {
   double* U0 = nullptr;     // [nc] x 4 state at the start of the step
   double* F = nullptr;      // [nc] x 4 RK accumulator (fcvar)
   void* Pv = nullptr;       // [nc] x 4 primitives (T)
+  void* Pv2 = nullptr;      // [nc] x 4 second primitive buffer of the fused first-order
+                            // stage (mixed batches; null: separate flux and update phases)
   void* Gx = nullptr;       // [nc] x 4 d/dx primitives (T)
   void* Gy = nullptr;       // [nc] x 4 d/dy primitives (T)
   void* phi = nullptr;      // [nc] limiter (T)
@@ -216,6 +218,8 @@ struct DcView {
   float* D0 = nullptr;   // correction at the start of the step
   float* DF = nullptr;   // stage accumulator (fcvar)
   float* dP = nullptr;   // primitive tangent of dU at the base state
+  float* dP2 = nullptr;  // second tangent buffer of the fused stage (null: separate
+                         // J dU and update phases)
   float* R0 = nullptr;   // FP64 residual of the base state, rounded to FP32
   float* dtl = nullptr;  // [nc] local time step at the base state (FP32)
 };
@@ -227,7 +231,7 @@ struct DcKernels {
   // the FP64 wave speeds (all cells)
   void (*base)(const DevView& d32, const DcView& c, const double* U64, const double* resid64, const double* ws64,
                cudaStream_t);
-  int (*occupancy)(int block);
+  int (*occupancy)(const DcView& c, int block);
   cudaError_t (*persistent)(const DevView& d32, const PersistPlan& p, const DcView& c, int grid, int block,
                             cudaStream_t);
   cudaError_t (*tiled_step)(const DevView& d32, const PersistPlan& p, const DcView& c, int block, cudaStream_t);

@@ -732,10 +732,11 @@ __device__ __forceinline__ void cell_residual_f(const DevView& d, int ic, bool w
   ws = wh + wl;
 }
 
+// the RK stage of one cell from its residual res (and, at a steady first
+// stage, its wave-speed sum ws); the new primitives go to Pout
 template <int MODE, bool COH>
-__device__ __forceinline__ void update_item(const DevView& d, const StageParams& sp, int ic, double* d2) {
-  float res[4], ws;
-  cell_residual_f(d, ic, sp.steady && sp.stage == 1, res, ws);
+__device__ __forceinline__ void apply_stage_f(const DevView& d, const StageParams& sp, int ic, const float* res,
+                                              float ws, float* Pout, double* d2) {
   float h = float(sp.h);
   if (sp.steady) {
     float dtl;
@@ -798,14 +799,22 @@ __device__ __forceinline__ void update_item(const DevView& d, const StageParams&
     }
   }
   st4(d.U, ic, u);
-  T p[4];
+  float p[4];
   cons2prim(TP(gm1), u, p);
-  st4(static_cast<T*>(d.Pv), ic, p);
+  st4(Pout, ic, p);
   if (sp.last) {
 #pragma unroll
     for (int v = 0; v < 4; v++) d2[v] += f2d_bits(inc[v] * inc[v]);
   }
 }
+
+template <int MODE, bool COH>
+__device__ __forceinline__ void update_item(const DevView& d, const StageParams& sp, int ic, double* d2) {
+  float res[4], ws;
+  cell_residual_f(d, ic, sp.steady && sp.stage == 1, res, ws);
+  apply_stage_f<MODE, COH>(d, sp, ic, res, ws, static_cast<float*>(d.Pv), d2);
+}
+
 #else
 // one cell of an RK stage; at the last stage adds |U-U0|^2 to d2
 template <int MODE, bool COH>
@@ -1004,6 +1013,24 @@ __device__ __forceinline__ void update_tile(const DevView& d, const PersistPlan&
   }
 }
 
+// per-case RMS(dU) of a step from the tile partials (fixed order), one block
+// per case; the partials are rewritten only at the next step's last stage
+__device__ __forceinline__ void case_norms_of_step(const PersistPlan& p, int step) {
+  const int slot = step % p.norm_cap;
+  for (int c = blockIdx.x; c < p.ncase_active; c += gridDim.x) {
+    if (threadIdx.x == 0) {
+      const int4 ct = p.case_tiles[c];
+      double a[4] = {0.0, 0.0, 0.0, 0.0};
+      for (int t = ct.y; t < ct.z; t++)
+#pragma unroll
+        for (int k = 0; k < 4; k++) a[k] += p.tile_partials[4 * (size_t)t + k];
+      double* o = p.case_norms + 4 * ((size_t)ct.x * p.norm_cap + slot);
+#pragma unroll
+      for (int k = 0; k < 4; k++) o[k] = sqrt(a[k] / double(ct.w));
+    }
+  }
+}
+
 template <int LIM, int REC>
 __global__ void __launch_bounds__(256) k_persistent(const DevView d, const PersistPlan p) {
   const int nb = gridDim.x;
@@ -1031,23 +1058,163 @@ __global__ void __launch_bounds__(256) k_persistent(const DevView d, const Persi
       }
       if (!grid_sync(p.bar, p.budget)) return;
     }
-    // per-case RMS(dU) of this step from the tile partials (fixed order); the
-    // partials are rewritten only at the next step's last update phase
-    const int slot = (step0 + s) % p.norm_cap;
-    for (int c = blockIdx.x; c < p.ncase_active; c += nb) {
-      if (threadIdx.x == 0) {
-        const int4 ct = p.case_tiles[c];
-        double a[4] = {0.0, 0.0, 0.0, 0.0};
-        for (int t = ct.y; t < ct.z; t++)
-#pragma unroll
-          for (int k = 0; k < 4; k++) a[k] += p.tile_partials[4 * (size_t)t + k];
-        double* o = p.case_norms + 4 * ((size_t)ct.x * p.norm_cap + slot);
-#pragma unroll
-        for (int k = 0; k < 4; k++) o[k] = sqrt(a[k] / double(ct.w));
-      }
-    }
+    case_norms_of_step(p, step0 + s);
   }
 }
+
+#if FVS_MIXED
+// One face of a cell for the fused first-order stage: the cell's signed
+// slot s (0: none; > 0: the cell is the edge's L), the other cell nb (-1 on
+// a boundary edge), its primitives, and the edge's normal and area.
+struct FaceRec {
+  float p[4];
+  T2 n;
+  float af;
+  int s, nb;
+};
+
+__device__ __forceinline__ void load_face(const DevView& d, const float* P, int s, FaceRec& r) {
+  r.s = s;
+  r.nb = -1;
+  if (s == 0) return;
+  const int e = (s > 0 ? s : -s) - 1;
+  const int2 lr = d.ecell[e];
+  r.nb = s > 0 ? lr.y : lr.x;
+  r.n = ld2(d.enrm, e);
+  r.af = static_cast<const float*>(d.earea)[e];
+  if (r.nb >= 0) ldc4<true>(P, r.nb, r.p);
+}
+
+// Roe flux x area and wave speed x area of a face in the edge's own
+// orientation (L, R, n), pc the cell's primitives: the REC_FIRST branch of
+// flux_item with the same operands
+__device__ __forceinline__ void face_flux_first(const DevView& d, const float* pc, const FaceRec& r, double time,
+                                                float* flux, float& wsa) {
+  float pfL[4], pfR[4];
+  if (r.s > 0) {
+#pragma unroll
+    for (int v = 0; v < 4; v++) pfL[v] = pc[v];
+    if (r.nb >= 0) {
+#pragma unroll
+      for (int v = 0; v < 4; v++) pfR[v] = r.p[v];
+    } else {
+      const int e = r.s - 1;
+      const T2 xy = ld2(d.exy, e);
+      ghost_state(d, d.ebtype[e], time, xy.x, xy.y, r.n.x, r.n.y, pfL, pfR);
+    }
+  } else {
+#pragma unroll
+    for (int v = 0; v < 4; v++) {
+      pfL[v] = r.p[v];
+      pfR[v] = pc[v];
+    }
+  }
+  float wsm;
+  roe_flux_fast(TP(gamma), TP(gm1), TP(igm1), pfL, pfR, r.n.x, r.n.y, flux, wsm);
+#pragma unroll
+  for (int v = 0; v < 4; v++) flux[v] = flux[v] * r.af;
+  wsa = wsm * r.af;
+}
+
+// Fused first-order stage of one cell: the fluxes of its own faces, summed
+// in its slot order as cell_residual_f sums the edge records, then the RK
+// stage.  An interior face is evaluated by both of its cells with the same
+// operands and the edge's own orientation (L, R, n).  All face records are
+// loaded first (independent loads); the flux loop is kept rolled, shifting
+// the records down one place per pass, so that every face runs the same
+// instructions and the two cells receive bit-identical fluxes of opposite
+// sign.
+template <int MODE>
+__device__ __forceinline__ void cell_stage_item(const DevView& d, const StageParams& sp, const float* Pin,
+                                                float* Pout, int ic, double time, double* d2) {
+  const int4 cf = d.cflist[ic];
+  FaceRec f0, f1, f2, f3;
+  load_face(d, Pin, cf.x, f0);
+  load_face(d, Pin, cf.y, f1);
+  load_face(d, Pin, cf.z, f2);
+  load_face(d, Pin, cf.w, f3);
+  float pc[4];
+  ldc4<true>(Pin, ic, pc);
+  float hi[4] = {0.f, 0.f, 0.f, 0.f}, lo[4] = {0.f, 0.f, 0.f, 0.f}, wh = 0.f, wl = 0.f;
+  const bool want_ws = sp.steady && sp.stage == 1;
+#pragma unroll 1
+  for (int j = 0; j < 4; j++) {
+    if (f0.s != 0) {
+      float f[4], wsa;
+      face_flux_first(d, pc, f0, time, f, wsa);
+#pragma unroll
+      for (int v = 0; v < 4; v++) two_sum(hi[v], lo[v], f0.s > 0 ? f[v] : -f[v]);
+      if (want_ws) two_sum(wh, wl, wsa);
+    }
+    f0 = f1;
+    f1 = f2;
+    f2 = f3;
+    f3.s = 0;
+  }
+  const float rv = -static_cast<const float*>(d.volT)[ic];
+  float res[4];
+#pragma unroll
+  for (int v = 0; v < 4; v++) res[v] = (hi[v] + lo[v]) * rv;
+  apply_stage_f<MODE, true>(d, sp, ic, res, wh + wl, Pout, d2);
+}
+
+template <int MODE>
+__device__ __forceinline__ void cell_stage_tile(const DevView& d, const PersistPlan& p, const StageParams& sp,
+                                                const float* Pin, float* Pout, int t, double time) {
+  const int4 tl = p.cell_tiles[t];
+  double d2[4] = {0.0, 0.0, 0.0, 0.0};
+  for (int ic = tl.x + threadIdx.x; ic < tl.y; ic += blockDim.x) cell_stage_item<MODE>(d, sp, Pin, Pout, ic, time, d2);
+  if (sp.last) {
+    double out[4];
+    block_sum4(d2, out);
+    if (threadIdx.x == 0)
+#pragma unroll
+      for (int k = 0; k < 4; k++) p.tile_partials[4 * (size_t)t + k] = out[k];
+  }
+}
+
+// primitives read by stage k (0-based) and written by it: Pv and Pv2 in
+// turn, so that with an even stage count every step ends in Pv
+__device__ __forceinline__ const float* stage_pin(const DevView& d, int k) {
+  return static_cast<const float*>((k & 1) ? d.Pv2 : d.Pv);
+}
+__device__ __forceinline__ float* stage_pout(const DevView& d, int k) {
+  return static_cast<float*>((k & 1) ? d.Pv : d.Pv2);
+}
+
+template <int MODE>
+__device__ __forceinline__ void cell_stage_phase(const DevView& d, const PersistPlan& p, int k, double time) {
+  for (int t = blockIdx.x; t < p.ncell_tiles; t += gridDim.x)
+    cell_stage_tile<MODE>(d, p, p.sp[k], stage_pin(d, k), stage_pout(d, k), t, time);
+}
+
+// First-order mixed stages with the flux evaluated per cell: one phase and
+// one grid barrier per stage instead of a flux phase and an update phase,
+// and no edge flux records in memory.
+// (every stage of a scheme has the same MODE)
+template <int MODE>
+__global__ void __launch_bounds__(256, 2) k_persistent_cell(const DevView d, const PersistPlan p) {
+  const int step0 = *p.step0_dev;
+  for (int s = 0; s < p.nsteps; s++) {
+    const double told = p.t1 + double(step0 + s) * d.dt;
+    for (int k = 0; k < p.nstages; k++) {
+      cell_stage_phase<MODE>(d, p, k, told + p.sp[k].dts);
+      if (!grid_sync(p.bar, p.budget)) return;
+    }
+    case_norms_of_step(p, step0 + s);
+  }
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(256, 2) k_tiles_cell(const DevView d, const PersistPlan p, int k) {
+  const double time = p.t1 + double(*p.step0_dev) * d.dt + p.sp[k].dts;
+  cell_stage_tile<MODE>(d, p, p.sp[k], stage_pin(d, k), stage_pout(d, k), blockIdx.x, time);
+}
+#endif
+
+// the fused first-order stage is in use (the host sets Pv2 only for
+// first-order mixed batches with an even number of stages)
+static inline bool cell_fused(const DevView& d) { return FVS_MIXED && d.Pv2 != nullptr && d.first_order; }
 
 template <int LIM, int REC>
 static cudaError_t launch_persistent_t(const DevView& d, const PersistPlan& p, int grid, int block, cudaStream_t s) {
@@ -1071,6 +1238,12 @@ static int persistent_occupancy(const DevView& d, int block) {
   if (d.grad_method != FVS_GRAD_LSQ) return 0;
   int n = 0;
   cudaError_t e;
+#if FVS_MIXED
+  if (cell_fused(d)) {
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_persistent_cell<MODE_SSP42>, block, 0);
+    return e == cudaSuccess ? n : 0;
+  }
+#endif
   if (d.first_order) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_persistent<0, REC_FIRST>, block, 0);
   else if (d.limiter != FVS_LIM_NONE)
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_persistent<1, REC_GENERAL>, block, 0);
@@ -1080,6 +1253,22 @@ static int persistent_occupancy(const DevView& d, int block) {
 }
 
 static cudaError_t launch_persistent(const DevView& d, const PersistPlan& p, int grid, int block, cudaStream_t s) {
+#if FVS_MIXED
+  if (cell_fused(d)) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3((unsigned)block);
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    if (p.sp[0].mode == MODE_SSP42) return cudaLaunchKernelEx(&cfg, k_persistent_cell<MODE_SSP42>, d, p);
+    if (p.sp[0].mode == MODE_SSP3) return cudaLaunchKernelEx(&cfg, k_persistent_cell<MODE_SSP3>, d, p);
+    return cudaLaunchKernelEx(&cfg, k_persistent_cell<MODE_RK>, d, p);
+  }
+#endif
   if (d.first_order) return launch_persistent_t<0, REC_FIRST>(d, p, grid, block, s);
   if (d.limiter != FVS_LIM_NONE) return launch_persistent_t<1, REC_GENERAL>(d, p, grid, block, s);
   if (persistent_spec(d)) return launch_persistent_t<0, REC_SPEC>(d, p, grid, block, s);
@@ -1133,6 +1322,19 @@ __global__ void __launch_bounds__(32) k_tiles_norms(const PersistPlan p) {
 }
 
 static cudaError_t launch_tiled_step(const DevView& d, const PersistPlan& p, int block, cudaStream_t s) {
+#if FVS_MIXED
+  if (cell_fused(d)) {
+    for (int k = 0; k < p.nstages; k++) {
+      switch (p.sp[k].mode) {
+        case MODE_SSP42: k_tiles_cell<MODE_SSP42><<<p.ncell_tiles, block, 0, s>>>(d, p, k); break;
+        case MODE_SSP3: k_tiles_cell<MODE_SSP3><<<p.ncell_tiles, block, 0, s>>>(d, p, k); break;
+        default: k_tiles_cell<MODE_RK><<<p.ncell_tiles, block, 0, s>>>(d, p, k); break;
+      }
+    }
+    k_tiles_norms<<<p.ncase_active, 32, 0, s>>>(p);
+    return cudaGetLastError();
+  }
+#endif
   for (int k = 0; k < p.nstages; k++) {
     if (!d.first_order) {
       if (d.limiter != FVS_LIM_NONE) k_tiles_gradient<1><<<p.ncell_tiles, block, 0, s>>>(d, p);
@@ -1220,36 +1422,30 @@ __device__ __forceinline__ Dual dsqrt_(Dual a) {
 __device__ __forceinline__ Dual dabs_(Dual a) { return a.v < 0.f ? -a : a; }
 __device__ __forceinline__ Dual half(Dual a) { return Dual(0.5f * a.v, 0.5f * a.d); }
 
-// J dU of one edge slot (first order: face states are the cell states),
-// times the face area, into the slot's flux record
-__device__ __forceinline__ void dc_flux_item(const DevView& d, const DcView& c, int e) {
-  const float* P = static_cast<const float*>(d.Pv);
-  const int2 lr = d.ecell[e];
-  const T2 n = ld2(d.enrm, e);
-  const float af = static_cast<const float*>(d.earea)[e];
-  float pl[4], ql[4], pr[4], qr[4];
-  ld4(P, lr.x, pl);
-  ldc4<true>(c.dP, lr.x, ql);
-  if (lr.y >= 0) {
-    ld4(P, lr.y, pr);
-    ldc4<true>(c.dP, lr.y, qr);
+// ghost state of boundary slot e and its tangent: the slip-wall mirror is
+// linear in the interior state; free-stream and Dirichlet ghost states do not
+// depend on it
+__device__ __forceinline__ void dc_ghost(const DevView& d, int e, T2 n, const float* pl, const float* ql, float* pr,
+                                         float* qr) {
+  const int rec = d.ebtype[e];
+  const T2 xy = ld2(d.exy, e);
+  ghost_state(d, rec, 0.0, xy.x, xy.y, n.x, n.y, pl, pr);
+  if ((rec & 15) == FVS_BC_SLIP_WALL) {
+    const float un = ql[1] * n.x + ql[2] * n.y;
+    qr[0] = ql[0];
+    qr[1] = ql[1] - 2.0f * un * n.x;
+    qr[2] = ql[2] - 2.0f * un * n.y;
+    qr[3] = ql[3];
   } else {
-    const int rec = d.ebtype[e];
-    const T2 xy = ld2(d.exy, e);
-    ghost_state(d, rec, 0.0, xy.x, xy.y, n.x, n.y, pl, pr);
-    if ((rec & 15) == FVS_BC_SLIP_WALL) {
-      // the mirror state is linear in the interior state
-      const float un = ql[1] * n.x + ql[2] * n.y;
-      qr[0] = ql[0];
-      qr[1] = ql[1] - 2.0f * un * n.x;
-      qr[2] = ql[2] - 2.0f * un * n.y;
-      qr[3] = ql[3];
-    } else {
-      // free stream and Dirichlet ghost states do not depend on the interior
 #pragma unroll
-      for (int v = 0; v < 4; v++) qr[v] = 0.0f;
-    }
+    for (int v = 0; v < 4; v++) qr[v] = 0.0f;
   }
+}
+
+// tangent of the Roe flux at (pl, pr) in the direction (ql, qr), times the
+// face area
+__device__ __forceinline__ void dc_jvp_core(const DevView& d, const float* pl, const float* ql, const float* pr,
+                                            const float* qr, T2 n, float af, float* f) {
   Dual L[4], R[4], F[4], wsm;
 #pragma unroll
   for (int v = 0; v < 4; v++) {
@@ -1257,7 +1453,33 @@ __device__ __forceinline__ void dc_flux_item(const DevView& d, const DcView& c, 
     R[v] = Dual(pr[v], qr[v]);
   }
   roe_flux_fast_t<Dual>(Dual(TP(gamma)), Dual(TP(gm1)), Dual(TP(igm1)), L, R, Dual(n.x), Dual(n.y), F, wsm);
-  const float f[4] = {F[0].d * af, F[1].d * af, F[2].d * af, F[3].d * af};
+#pragma unroll
+  for (int v = 0; v < 4; v++) f[v] = F[v].d * af;
+}
+
+// J dU of one edge slot (first order: face states are the cell states),
+// times the face area; primitive tangents read from dP
+__device__ __forceinline__ void dc_edge_jvp(const DevView& d, const float* dP, int e, float* f) {
+  const float* P = static_cast<const float*>(d.Pv);
+  const int2 lr = d.ecell[e];
+  const T2 n = ld2(d.enrm, e);
+  const float af = static_cast<const float*>(d.earea)[e];
+  float pl[4], ql[4], pr[4], qr[4];
+  ld4(P, lr.x, pl);
+  ldc4<true>(dP, lr.x, ql);
+  if (lr.y >= 0) {
+    ld4(P, lr.y, pr);
+    ldc4<true>(dP, lr.y, qr);
+  } else {
+    dc_ghost(d, e, n, pl, ql, pr, qr);
+  }
+  dc_jvp_core(d, pl, ql, pr, qr, n, af, f);
+}
+
+// J dU of one edge slot into the slot's flux record
+__device__ __forceinline__ void dc_flux_item(const DevView& d, const DcView& c, int e) {
+  float f[4];
+  dc_edge_jvp(d, c.dP, e, f);
   st4(static_cast<float*>(d.eflux), e, f);
 }
 
@@ -1266,20 +1488,8 @@ __device__ __forceinline__ void dc_flux_item(const DevView& d, const DcView& c, 
 // writes the primitive tangent of the new dU and, at the last stage, adds
 // |dU - dU0|^2 to d2.
 template <int MODE>
-__device__ __forceinline__ void dc_update_item(const DevView& d, const DcView& c, const StageParams& sp, int ic,
-                                               float* d2) {
-  float acc[4] = {0.f, 0.f, 0.f, 0.f};
-  const int4 cf = d.cflist[ic];
-  const int sl[4] = {cf.x, cf.y, cf.z, cf.w};
-#pragma unroll
-  for (int j = 0; j < 4; j++) {
-    const int s = sl[j];
-    if (s == 0) continue;
-    float f[4];
-    ldc4<true>(static_cast<const float*>(d.eflux), (s > 0 ? s : -s) - 1, f);
-#pragma unroll
-    for (int v = 0; v < 4; v++) acc[v] += s > 0 ? f[v] : -f[v];
-  }
+__device__ __forceinline__ void dc_apply_stage(const DevView& d, const DcView& c, const StageParams& sp, int ic,
+                                               const float* acc, float* dPout, float* d2) {
   const float rv = -static_cast<const float*>(d.volT)[ic];
   float r0[4], res[4];
   ld4(c.R0, ic, r0);
@@ -1319,7 +1529,7 @@ __device__ __forceinline__ void dc_update_item(const DevView& d, const DcView& c
   const float du = (u[1] - p[1] * u[0]) * ri, dv = (u[2] - p[2] * u[0]) * ri;
   const float q[4] = {u[0], du, dv,
                       d.fgm1 * (u[3] - 0.5f * u[0] * (p[1] * p[1] + p[2] * p[2]) - p[0] * (p[1] * du + p[2] * dv))};
-  st4(c.dP, ic, q);
+  st4(dPout, ic, q);
   if (sp.last) {
 #pragma unroll
     for (int v = 0; v < 4; v++) {
@@ -1330,46 +1540,169 @@ __device__ __forceinline__ void dc_update_item(const DevView& d, const DcView& c
 }
 
 template <int MODE>
+__device__ __forceinline__ void dc_update_item(const DevView& d, const DcView& c, const StageParams& sp, int ic,
+                                               float* d2) {
+  float acc[4] = {0.f, 0.f, 0.f, 0.f};
+  const int4 cf = d.cflist[ic];
+  const int sl[4] = {cf.x, cf.y, cf.z, cf.w};
+#pragma unroll
+  for (int j = 0; j < 4; j++) {
+    const int s = sl[j];
+    if (s == 0) continue;
+    float f[4];
+    ldc4<true>(static_cast<const float*>(d.eflux), (s > 0 ? s : -s) - 1, f);
+#pragma unroll
+    for (int v = 0; v < 4; v++) acc[v] += s > 0 ? f[v] : -f[v];
+  }
+  dc_apply_stage<MODE>(d, c, sp, ic, acc, c.dP, d2);
+}
+
+// the correction tangents read and written by stage k (0-based) of the fused
+// stage: dP and dP2 in turn, so that with an even stage count every step
+// ends in dP
+__device__ __forceinline__ const float* dc_pin(const DcView& c, int k) { return (k & 1) ? c.dP2 : c.dP; }
+__device__ __forceinline__ float* dc_pout(const DcView& c, int k) { return (k & 1) ? c.dP : c.dP2; }
+
+// one face of a cell for the fused correction stage (as FaceRec, with the
+// other cell's base primitives p and tangent q)
+struct DcFace {
+  float p[4], q[4];
+  T2 n;
+  float af;
+  int s, nb;
+};
+
+__device__ __forceinline__ void load_dc_face(const DevView& d, const float* dP, int s, DcFace& r) {
+  r.s = s;
+  r.nb = -1;
+  if (s == 0) return;
+  const int e = (s > 0 ? s : -s) - 1;
+  const int2 lr = d.ecell[e];
+  r.nb = s > 0 ? lr.y : lr.x;
+  r.n = ld2(d.enrm, e);
+  r.af = static_cast<const float*>(d.earea)[e];
+  if (r.nb >= 0) {
+    ld4(static_cast<const float*>(d.Pv), r.nb, r.p);
+    ldc4<true>(dP, r.nb, r.q);
+  }
+}
+
+// J dU of a face in the edge's own orientation; (pc, qc) the cell's base
+// primitives and tangent
+__device__ __forceinline__ void dc_face_jvp(const DevView& d, const float* pc, const float* qc, const DcFace& r,
+                                            float* f) {
+  float pl[4], ql[4], pr[4], qr[4];
+  if (r.s > 0) {
+#pragma unroll
+    for (int v = 0; v < 4; v++) {
+      pl[v] = pc[v];
+      ql[v] = qc[v];
+    }
+    if (r.nb >= 0) {
+#pragma unroll
+      for (int v = 0; v < 4; v++) {
+        pr[v] = r.p[v];
+        qr[v] = r.q[v];
+      }
+    } else {
+      dc_ghost(d, r.s - 1, r.n, pl, ql, pr, qr);
+    }
+  } else {
+#pragma unroll
+    for (int v = 0; v < 4; v++) {
+      pl[v] = r.p[v];
+      ql[v] = r.q[v];
+      pr[v] = pc[v];
+      qr[v] = qc[v];
+    }
+  }
+  dc_jvp_core(d, pl, ql, pr, qr, r.n, r.af, f);
+}
+
+// Fused correction stage of one cell: J dU of its own faces (each interior
+// face evaluated by both cells in the edge's orientation; records loaded
+// first and the loop kept rolled, as in cell_stage_item), summed in slot
+// order, then the stage.
+template <int MODE>
+__device__ __forceinline__ void dc_cell_item(const DevView& d, const DcView& c, const StageParams& sp,
+                                             const float* dPin, float* dPout, int ic, float* d2) {
+  const int4 cf = d.cflist[ic];
+  DcFace f0, f1, f2, f3;
+  load_dc_face(d, dPin, cf.x, f0);
+  load_dc_face(d, dPin, cf.y, f1);
+  load_dc_face(d, dPin, cf.z, f2);
+  load_dc_face(d, dPin, cf.w, f3);
+  float pc[4], qc[4];
+  ld4(static_cast<const float*>(d.Pv), ic, pc);
+  ldc4<true>(dPin, ic, qc);
+  float acc[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll 1
+  for (int j = 0; j < 4; j++) {
+    if (f0.s != 0) {
+      float f[4];
+      dc_face_jvp(d, pc, qc, f0, f);
+#pragma unroll
+      for (int v = 0; v < 4; v++) acc[v] += f0.s > 0 ? f[v] : -f[v];
+    }
+    f0 = f1;
+    f1 = f2;
+    f2 = f3;
+    f3.s = 0;
+  }
+  dc_apply_stage<MODE>(d, c, sp, ic, acc, dPout, d2);
+}
+
+// One cell tile of a correction stage (FUSED: with the cell's own face
+// J dU; otherwise from the edge records of a separate J dU phase) and, at
+// the last stage, the tile's partial sums of |dU - dU0|^2
+template <int MODE, bool FUSED>
+__device__ __forceinline__ void dc_stage_tile(const DevView& d, const DcView& c, const PersistPlan& p, int k, int t) {
+  const StageParams& sp = p.sp[k];
+  const int4 tl = p.cell_tiles[t];
+  float d2f[4] = {0.f, 0.f, 0.f, 0.f};
+  for (int ic = tl.x + threadIdx.x; ic < tl.y; ic += blockDim.x) {
+    if (FUSED) dc_cell_item<MODE>(d, c, sp, dc_pin(c, k), dc_pout(c, k), ic, d2f);
+    else dc_update_item<MODE>(d, c, sp, ic, d2f);
+  }
+  if (sp.last) {
+    const double d2[4] = {f2d_bits(d2f[0]), f2d_bits(d2f[1]), f2d_bits(d2f[2]), f2d_bits(d2f[3])};
+    double out[4];
+    block_sum4(d2, out);
+    if (threadIdx.x == 0)
+#pragma unroll
+      for (int q = 0; q < 4; q++) p.tile_partials[4 * (size_t)t + q] = out[q];
+  }
+}
+
+template <int MODE>
 __global__ void __launch_bounds__(256, 3) k_persistent_dc(const DevView d, const PersistPlan p, const DcView c) {
   const int nb = gridDim.x;
   const int step0 = *p.step0_dev;
   for (int s = 0; s < p.nsteps; s++) {
     for (int k = 0; k < p.nstages; k++) {
-      const StageParams& sp = p.sp[k];
       for (int t = blockIdx.x; t < p.nedge_tiles; t += nb) {
         const int2 tl = p.edge_tiles[t];
         for (int e = tl.x + threadIdx.x; e < tl.y; e += blockDim.x) dc_flux_item(d, c, e);
       }
       if (!grid_sync(p.bar, p.budget)) return;
-      for (int t = blockIdx.x; t < p.ncell_tiles; t += nb) {
-        const int4 tl = p.cell_tiles[t];
-        float d2f[4] = {0.f, 0.f, 0.f, 0.f};
-        for (int ic = tl.x + threadIdx.x; ic < tl.y; ic += blockDim.x) dc_update_item<MODE>(d, c, sp, ic, d2f);
-        if (sp.last) {
-          const double d2[4] = {f2d_bits(d2f[0]), f2d_bits(d2f[1]), f2d_bits(d2f[2]), f2d_bits(d2f[3])};
-          double out[4];
-          block_sum4(d2, out);
-          if (threadIdx.x == 0)
-#pragma unroll
-            for (int q = 0; q < 4; q++) p.tile_partials[4 * (size_t)t + q] = out[q];
-        }
-      }
+      for (int t = blockIdx.x; t < p.ncell_tiles; t += nb) dc_stage_tile<MODE, false>(d, c, p, k, t);
       if (!grid_sync(p.bar, p.budget)) return;
     }
     // per-case RMS of the correction increments of this step (fixed order)
-    const int slot = (step0 + s) % p.norm_cap;
-    for (int cs = blockIdx.x; cs < p.ncase_active; cs += nb) {
-      if (threadIdx.x == 0) {
-        const int4 ct = p.case_tiles[cs];
-        double a[4] = {0.0, 0.0, 0.0, 0.0};
-        for (int t = ct.y; t < ct.z; t++)
-#pragma unroll
-          for (int q = 0; q < 4; q++) a[q] += p.tile_partials[4 * (size_t)t + q];
-        double* o = p.case_norms + 4 * ((size_t)ct.x * p.norm_cap + slot);
-#pragma unroll
-        for (int q = 0; q < 4; q++) o[q] = sqrt(a[q] / double(ct.w));
-      }
+    case_norms_of_step(p, step0 + s);
+  }
+}
+
+// fused correction stages: one phase and one grid barrier per stage
+template <int MODE>
+__global__ void __launch_bounds__(256, 2) k_persistent_dc_cell(const DevView d, const PersistPlan p, const DcView c) {
+  const int step0 = *p.step0_dev;
+  for (int s = 0; s < p.nsteps; s++) {
+    for (int k = 0; k < p.nstages; k++) {
+      for (int t = blockIdx.x; t < p.ncell_tiles; t += gridDim.x) dc_stage_tile<MODE, true>(d, c, p, k, t);
+      if (!grid_sync(p.bar, p.budget)) return;
     }
+    case_norms_of_step(p, step0 + s);
   }
 }
 
@@ -1412,10 +1745,12 @@ static void dc_base(const DevView& d, const DcView& c, const double* U64, const 
                     cudaStream_t s) {
   k_dc_base<<<grid_of(d.nc), 256, 0, s>>>(d, c, U64, resid64, ws64);
 }
-static int dc_occupancy(int block) {
+static int dc_occupancy(const DcView& c, int block) {
   int n = 0;
-  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_persistent_dc<MODE_SSP42>, block, 0) == cudaSuccess ? n
-                                                                                                               : 0;
+  const cudaError_t e =
+      c.dP2 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_persistent_dc_cell<MODE_SSP42>, block, 0)
+            : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_persistent_dc<MODE_SSP42>, block, 0);
+  return e == cudaSuccess ? n : 0;
 }
 static cudaError_t dc_persistent(const DevView& d, const PersistPlan& p, const DcView& c, int grid, int block,
                                  cudaStream_t s) {
@@ -1428,6 +1763,10 @@ static cudaError_t dc_persistent(const DevView& d, const PersistPlan& p, const D
   attr[0].val.cooperative = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
+  if (c.dP2) {
+    if (p.sp[0].mode == MODE_SSP42) return cudaLaunchKernelEx(&cfg, k_persistent_dc_cell<MODE_SSP42>, d, p, c);
+    return cudaLaunchKernelEx(&cfg, k_persistent_dc_cell<MODE_RK>, d, p, c);
+  }
   if (p.sp[0].mode == MODE_SSP42) return cudaLaunchKernelEx(&cfg, k_persistent_dc<MODE_SSP42>, d, p, c);
   return cudaLaunchKernelEx(&cfg, k_persistent_dc<MODE_RK>, d, p, c);
 }
@@ -1437,29 +1776,22 @@ __global__ void __launch_bounds__(256) k_tiles_dc_flux(const DevView d, const Dc
   for (int e = tl.x + threadIdx.x; e < tl.y; e += blockDim.x) dc_flux_item(d, c, e);
 }
 
-template <int MODE>
+template <int MODE, bool FUSED>
 __global__ void __launch_bounds__(256) k_tiles_dc_update(const DevView d, const DcView c, const PersistPlan p,
                                                          int stage) {
-  const StageParams& sp = p.sp[stage];
-  const int t = blockIdx.x;
-  const int4 tl = p.cell_tiles[t];
-  float d2f[4] = {0.f, 0.f, 0.f, 0.f};
-  for (int ic = tl.x + threadIdx.x; ic < tl.y; ic += blockDim.x) dc_update_item<MODE>(d, c, sp, ic, d2f);
-  if (sp.last) {
-    const double d2[4] = {f2d_bits(d2f[0]), f2d_bits(d2f[1]), f2d_bits(d2f[2]), f2d_bits(d2f[3])};
-    double out[4];
-    block_sum4(d2, out);
-    if (threadIdx.x == 0)
-#pragma unroll
-      for (int q = 0; q < 4; q++) p.tile_partials[4 * (size_t)t + q] = out[q];
-  }
+  dc_stage_tile<MODE, FUSED>(d, c, p, stage, blockIdx.x);
 }
 
 static cudaError_t dc_tiled_step(const DevView& d, const PersistPlan& p, const DcView& c, int block, cudaStream_t s) {
   for (int k = 0; k < p.nstages; k++) {
+    if (c.dP2) {
+      if (p.sp[k].mode == MODE_SSP42) k_tiles_dc_update<MODE_SSP42, true><<<p.ncell_tiles, block, 0, s>>>(d, c, p, k);
+      else k_tiles_dc_update<MODE_RK, true><<<p.ncell_tiles, block, 0, s>>>(d, c, p, k);
+      continue;
+    }
     k_tiles_dc_flux<<<p.nedge_tiles, block, 0, s>>>(d, c, p);
-    if (p.sp[k].mode == MODE_SSP42) k_tiles_dc_update<MODE_SSP42><<<p.ncell_tiles, block, 0, s>>>(d, c, p, k);
-    else k_tiles_dc_update<MODE_RK><<<p.ncell_tiles, block, 0, s>>>(d, c, p, k);
+    if (p.sp[k].mode == MODE_SSP42) k_tiles_dc_update<MODE_SSP42, false><<<p.ncell_tiles, block, 0, s>>>(d, c, p, k);
+    else k_tiles_dc_update<MODE_RK, false><<<p.ncell_tiles, block, 0, s>>>(d, c, p, k);
   }
   k_tiles_norms<<<p.ncase_active, 32, 0, s>>>(p);
   return cudaGetLastError();

@@ -90,7 +90,7 @@ def solve_ladder(meshes, opts_mixed, levels, switch=1e-5, drop=1e-10, max_steps=
         t1 = time.perf_counter()
         phases["setup"] = t1 - t0
         if autotune:
-            b.autotune(2)
+            b.autotune(10)
         t2 = time.perf_counter()
         phases["tune"] = t2 - t1
         n1, _, _, _ = b.run_to_level(max_steps, np.asarray(levels) * switch, chunk)

@@ -240,7 +240,8 @@ int fvs_batch_create(const fvs_mesh* meshes, const fvs_options* opts, int32_t nc
 void fvs_batch_destroy(fvs_batch* b);
 const char* fvs_batch_last_error(const fvs_batch* b);
 /* total cells and edge slots; launch4 = {block, tile, blocks per SM, flags}
- * with flags bit 0 = persistent launches graph-captured, bit 1 = tiled mode */
+ * with flags bit 0 = persistent launches graph-captured, bit 1 = tiled mode,
+ * bit 2 = fused first-order stages in use */
 int fvs_batch_info(const fvs_batch* b, int32_t* ncells, int32_t* nedges, int32_t* launch4);
 int fvs_batch_init_state(fvs_batch* b);                                  /* free stream per case */
 int fvs_batch_set_state(fvs_batch* b, int32_t icase, const double* cvar); /* [ncells_case][4] */
@@ -248,10 +249,20 @@ int fvs_batch_get_state(fvs_batch* b, int32_t icase, double* cvar);
 /* times the launch-shape candidates on the batch (state restored after) */
 int fvs_batch_autotune(fvs_batch* b, int32_t trial_steps, float* best_ms_per_step);
 int fvs_batch_set_launch(fvs_batch* b, int32_t block, int32_t tile, int32_t blocks_per_sm);
-/* 0: one cooperative persistent launch per chunk of steps (grid barriers
- * between phases); 1: each step a CUDA graph of tile launches, one block per
- * tile and phase.  fvs_batch_autotune times both. */
-int fvs_batch_set_mode(fvs_batch* b, int32_t tiled);
+/* mode 0: one cooperative persistent launch per chunk of steps (grid
+ * barriers between phases); FVS_BATCH_TILED: each step a CUDA graph of tile
+ * launches, one block per tile and phase (fvs_batch_autotune times both).
+ * First-order mixed-precision stages with an even number of stages are
+ * fused: each cell evaluates the flux of its own faces (every interior face
+ * twice, once from each side, in the edge's orientation) and applies the
+ * stage, one phase per stage; FVS_BATCH_UNFUSED keeps the separate edge-flux
+ * and update phases (the autotuner times both).  FVS_BATCH_DC_FUSED fuses the
+ * defect-correction stages the same way (off by default: slower than the
+ * separate phases on the measured sweeps). */
+#define FVS_BATCH_TILED 1
+#define FVS_BATCH_UNFUSED 2
+#define FVS_BATCH_DC_FUSED 4
+int fvs_batch_set_mode(fvs_batch* b, int32_t mode);
 /* switches the arithmetic of all cases (FVS_PREC_*), keeping the FP64
  * state: e.g. MIXED until the FP32 flux floor, then FP64 to a 1e-10 drop */
 int fvs_batch_set_precision(fvs_batch* b, int32_t precision);

@@ -138,6 +138,31 @@ def test_tiled_mode_equals_persistent(prec, first_order):
         assert np.allclose(nt, np_, rtol=1e-5, atol=0)
 
 
+@pytest.mark.parametrize("tiled", [False, True])
+def test_fused_first_order_stage_matches_separate_phases(tiled):
+    """First-order mixed batches evaluate each cell's face fluxes inside its
+    stage (one phase per stage).  Same flux and summation order as the
+    separate edge-flux and update phases: states agree to FP32 rounding of
+    the increments; the second-order batch is never fused."""
+    meshes, opts = sweep(prec=PREC_MIXED, reconst=1, limiter=0)
+    res = []
+    for fused in (False, True):
+        with Batch(meshes, opts) as b:
+            b.set_mode(tiled, fused=fused)
+            b.initialize_solution()
+            n1, _ = b.steps(40)
+            assert b.info()["fused"] == fused
+            res.append((n1, [b.get_state(c) for c in range(3)]))
+    for c in range(3):
+        assert rel(res[1][1][c], res[0][1][c]) <= 1e-6, (c, rel(res[1][1][c], res[0][1][c]))
+    assert np.allclose(res[1][0], res[0][0], rtol=1e-4, atol=0)
+    m2, o2 = sweep(1, prec=PREC_MIXED)
+    with Batch(m2, o2) as b:
+        b.initialize_solution()
+        b.steps(1)
+        assert not b.info()["fused"]
+
+
 def test_autotune_keeps_state_and_results():
     meshes, opts = sweep(3)
     with Batch(meshes, opts) as b:

@@ -69,6 +69,30 @@ def test_tiled_mode_equals_persistent():
     assert np.allclose(out[0][1], out[1][1], rtol=1e-6, atol=0)
 
 
+@pytest.mark.parametrize("tiled", [False, True])
+def test_fused_stage_matches_separate_phases(tiled):
+    """Defect correction with each cell's face J dU inside its stage (one
+    phase per stage) against separate J dU and update phases: the same
+    corrections up to FP32 rounding, and the same fixed point."""
+    meshes, opts = first_order_sweep(PREC_MIXED)
+    out = []
+    for fused in (False, True):
+        with Batch(meshes, opts) as b:
+            b.set_mode(tiled, dc_fused=fused)
+            b.initialize_solution()
+            b.steps(200)
+            u0 = [b.get_state(c) for c in range(3)]
+            never = np.zeros((3, 4))
+            done, _, last, _ = b.run_to_level(60, never, chunk=25, dc=True)
+            assert np.all(done == 60)
+            out.append(([b.get_state(c) for c in range(3)], last, u0))
+    for c in range(3):
+        a, t, s0 = out[0][0][c], out[1][0][c], out[0][2][c]
+        inc = np.abs(a - s0).max()
+        assert np.abs(a - t).max() <= 1e-4 * inc, (c, np.abs(a - t).max(), inc)
+    assert np.allclose(out[0][1], out[1][1], rtol=1e-3, atol=0)
+
+
 def test_converges_to_the_fp64_fixed_point():
     meshes, opts = first_order_sweep(PREC_MIXED)
     with Batch(meshes, opts) as b:
