@@ -103,13 +103,14 @@ class Batch:
                                                     capi.ptr(first), capi.ptr(last), C.byref(ms)))
         return done, first, last, ms.value
 
-    def set_mode(self, tiled: bool, fused: bool = True, dc_fused: bool = False) -> None:
+    def set_mode(self, tiled: bool, fused: bool = True, dc_fused: bool = False, fixed: bool = False) -> None:
         """Launch mode: a persistent cooperative kernel per chunk (tiled False)
         or a graph of per-phase tile launches per step (True).  fused: first-
         order mixed stages evaluate the flux per cell in one phase per stage
         (where the stage count is even); dc_fused: the same for the
-        defect-correction stages."""
-        mode = (1 if tiled else 0) | (0 if fused else 2) | (4 if dc_fused else 0)
+        defect-correction stages; fixed: run_to_level keeps this shape instead
+        of trying others as the active set shrinks."""
+        mode = (1 if tiled else 0) | (0 if fused else 2) | (4 if dc_fused else 0) | (8 if fixed else 0)
         self._check(self._lib.fvs_batch_set_mode(self._h, mode))
 
     def set_groups(self, group=None) -> None:

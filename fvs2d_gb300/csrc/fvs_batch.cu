@@ -105,6 +105,8 @@ struct fvs_batch {
   int graph_steps = -1;
   bool plan_dirty = true, use_graph = true;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  cudaEvent_t eva = nullptr, evb = nullptr;  // around one chunk's launches (shape trials)
+  bool retune = true;                         // shape trials as the active set shrinks
   int* h_step0 = nullptr;
   DcView dc;  // defect-correction arrays, allocated on first use
   // launch mode: false = one cooperative persistent launch per chunk, true =
@@ -126,6 +128,8 @@ struct fvs_batch {
     if (tgraph_dc) cudaGraphExecDestroy(tgraph_dc);
     if (ev0) cudaEventDestroy(ev0);
     if (ev1) cudaEventDestroy(ev1);
+    if (eva) cudaEventDestroy(eva);
+    if (evb) cudaEventDestroy(evb);
     if (h_step0) cudaFreeHost(h_step0);
     arena.release();
     if (stream) cudaStreamDestroy(stream);
@@ -346,8 +350,9 @@ int grid_size(fvs_batch* B) {
   return std::max(1, std::min(B->bps, occ)) * B->nsm;
 }
 
-// one chunk of nsteps steps starting at global step step0 (graph replay)
-int launch_chunk(fvs_batch* B, int nsteps, int step0) {
+// one chunk of nsteps steps starting at global step step0 (graph replay);
+// timed: events recorded on the stream around the chunk's launches
+int launch_chunk(fvs_batch* B, int nsteps, int step0, bool timed = false) {
   if (B->plan_dirty) {
     int rc = build_plan(B);
     if (rc) return rc;
@@ -364,7 +369,9 @@ int launch_chunk(fvs_batch* B, int nsteps, int step0) {
       if (e != cudaSuccess) return B->cuda_fail(e, "tiled step capture");
     }
     e = cudaMemsetAsync(B->d_bar, 0, sizeof(GridBarrier), B->stream);
+    if (timed) cudaEventRecord(B->eva, B->stream);
     for (int i = 0; i < nsteps && e == cudaSuccess; i++) e = cudaGraphLaunch(B->tgraph, B->stream);
+    if (timed) cudaEventRecord(B->evb, B->stream);
     return e == cudaSuccess ? FVS_OK : B->cuda_fail(e, "tiled step launch");
   }
   const int grid = grid_size(B);
@@ -394,6 +401,7 @@ int launch_chunk(fvs_batch* B, int nsteps, int step0) {
       B->graph_steps = nsteps;
     }
   }
+  if (timed) cudaEventRecord(B->eva, B->stream);
   if (B->use_graph) {
     e = cudaGraphLaunch(B->graph, B->stream);
     if (e != cudaSuccess) return B->cuda_fail(e, "cudaGraphLaunch");
@@ -402,8 +410,94 @@ int launch_chunk(fvs_batch* B, int nsteps, int step0) {
     if (e == cudaSuccess) e = B->ks->persistent(B->d, B->plan, grid, B->block, B->stream);
     if (e != cudaSuccess) return B->cuda_fail(e, "persistent launch");
   }
+  if (timed) cudaEventRecord(B->evb, B->stream);
   return FVS_OK;
 }
+
+// A launch shape of the batched kernels.
+struct LaunchShape {
+  bool tiled, fuse;
+  int block, tile, bps;
+};
+
+// Online choice of the launch shape as cases converge and the active set
+// shrinks (the best shape of a small set differs from that of the full
+// batch: fewer, shorter tiles, fewer blocks to synchronise).  Once the active
+// cells fall to half of those at the last choice (or at once, when `now`),
+// the next chunks run one candidate shape each for a few steps, timed on the
+// device, and the fastest is kept.  Every trial step is a step of the run:
+// nothing is repeated or discarded.
+class ShapeTrials {
+ public:
+  ShapeTrials(fvs_batch* b, bool dc, bool now) : b_(b) {
+    if (!b->retune) return;
+    const LaunchShape cur = {b->tiled, b->fuse, b->block, b->tile, b->bps};
+    cand_.push_back(cur);
+    const bool fz = !dc && b->prec == FVS_PREC_MIXED && fusable(b);
+    for (int f = 0; f < (fz ? 2 : 1); f++) {
+      const bool fuse = dc ? b->fuse : f == 1;
+      cand_.push_back({false, fuse, 256, 1024, 2});
+      cand_.push_back({false, fuse, 256, 256, 1});
+      cand_.push_back({false, fuse, 128, 256, 2});
+      cand_.push_back({true, fuse, 256, 1024, 1});
+      cand_.push_back({true, fuse, 128, 256, 1});
+    }
+    us_.assign(cand_.size(), 0.f);
+    cells_ = active_cells();
+    if (now) next_ = 0;
+  }
+  bool trialling() const { return next_ >= 0; }
+  // before a chunk: apply the candidate under trial; the chunk length
+  int before_chunk(int n) {
+    if (next_ < 0) return n;
+    apply(cand_[next_]);
+    return std::min(n, kTrialSteps);
+  }
+  // after a chunk of n steps, its events synchronised
+  void after_chunk(int n) {
+    if (next_ < 0) return;
+    float ms = 0.f;
+    cudaEventSynchronize(b_->evb);
+    cudaEventElapsedTime(&ms, b_->eva, b_->evb);
+    us_[next_] = 1000.f * ms / std::max(1, n);
+    if (++next_ < (int)cand_.size()) return;
+    int best = 0;
+    for (int k = 1; k < (int)cand_.size(); k++)
+      if (us_[k] < us_[best]) best = k;
+    apply(cand_[best]);
+    cand_[0] = cand_[best];
+    next_ = -1;
+  }
+  // after the active set changed
+  void active_changed() {
+    if (cand_.empty() || next_ >= 0) return;
+    const long long c = active_cells();
+    if (2 * c <= cells_) {
+      cells_ = c;
+      next_ = 0;
+    }
+  }
+
+ private:
+  static constexpr int kTrialSteps = 20;
+  long long active_cells() const {
+    long long n = 0;
+    for (int c = 0; c < b_->ncases; c++)
+      if (b_->active[c]) n += b_->cnum[c];
+    return n;
+  }
+  void apply(const LaunchShape& s) {
+    if (s.tiled == b_->tiled && s.fuse == b_->fuse && s.block == b_->block && s.tile == b_->tile && s.bps == b_->bps)
+      return;
+    b_->tiled = s.tiled; b_->fuse = s.fuse; b_->block = s.block; b_->tile = s.tile; b_->bps = s.bps;
+    b_->plan_dirty = true;
+  }
+  fvs_batch* b_;
+  std::vector<LaunchShape> cand_;
+  std::vector<float> us_;
+  long long cells_ = 0;
+  int next_ = -1;
+};
 
 // View of precision prec: the current one, or a variant built on first use
 // from the stored host meshes (same device order as every other variant).
@@ -454,8 +548,13 @@ int fvs_batch_create(const fvs_mesh* meshes, const fvs_options* opts, int32_t nc
       g_batch_create_error = "case " + std::to_string(c) + ": all cases of a batch share the scheme (only Mach and angle of attack differ)";
       return FVS_ERR_INVALID;
     }
-  if (o0.grad_method != FVS_GRAD_LSQ || o0.dt_from_cfl || o0.flux != 1 || o0.rk_nstages < 3 || o0.rk_nstages > 4) {
-    g_batch_create_error = "batches run LSQ gradients with a fixed dt (or steady)";
+  const char* unsupported = o0.grad_method != FVS_GRAD_LSQ             ? "batches run LSQ gradients"
+                            : o0.dt_from_cfl                            ? "batches run a fixed dt or steady time stepping"
+                            : o0.flux != 1                              ? "batches run the Roe flux"
+                            : (o0.rk_nstages < 3 || o0.rk_nstages > 4) ? "batches run 3- or 4-stage Runge-Kutta schemes"
+                                                                        : nullptr;
+  if (unsupported) {
+    g_batch_create_error = unsupported;
     return FVS_ERR_INVALID;
   }
   std::unique_ptr<fvs_batch> B(new fvs_batch());
@@ -501,6 +600,8 @@ int fvs_batch_create(const fvs_mesh* meshes, const fvs_options* opts, int32_t nc
   cudaMallocHost(&B->h_step0, 16);
   cudaEventCreate(&B->ev0);
   cudaEventCreate(&B->ev1);
+  cudaEventCreate(&B->eva);
+  cudaEventCreate(&B->evb);
   cudaDeviceGetAttribute(&B->nsm, cudaDevAttrMultiProcessorCount, 0);
   init_view_constants(B.get(), B->d);
   int rc = build_for(B.get(), B->prec, B->d);
@@ -622,10 +723,12 @@ int fvs_batch_set_groups(fvs_batch* b, const int32_t* group) {
 }
 
 int fvs_batch_set_mode(fvs_batch* b, int32_t mode) {
-  if (!b || mode < 0 || mode > (FVS_BATCH_TILED | FVS_BATCH_UNFUSED | FVS_BATCH_DC_FUSED)) return FVS_ERR_INVALID;
+  if (!b || mode < 0 || mode > (FVS_BATCH_TILED | FVS_BATCH_UNFUSED | FVS_BATCH_DC_FUSED | FVS_BATCH_FIXED_SHAPE))
+    return FVS_ERR_INVALID;
   b->tiled = (mode & FVS_BATCH_TILED) != 0;
   b->fuse = (mode & FVS_BATCH_UNFUSED) == 0;
   b->fuse_dc = (mode & FVS_BATCH_DC_FUSED) != 0;
+  b->retune = (mode & FVS_BATCH_FIXED_SHAPE) == 0;
   b->plan_dirty = true;
   return FVS_OK;
 }
@@ -749,9 +852,12 @@ static int run_until(fvs_batch* b, int32_t max_steps, double drop, const double*
   cudaEventRecord(b->ev0, b->stream);
   int step = 0, rc = FVS_OK;
   bool nonfinite = false;
+  // shapes chosen for a shrunken active set last for this run only
+  const LaunchShape start = {b->tiled, b->fuse, b->block, b->tile, b->bps};
+  ShapeTrials trials(b, false, false);
   while (step < max_steps) {
-    const int n = std::min(chunk, max_steps - step);
-    if ((rc = launch_chunk(b, n, step))) break;
+    const int n = trials.before_chunk(std::min(chunk, max_steps - step));
+    if ((rc = launch_chunk(b, n, step, trials.trialling()))) break;
     if ((rc = check_barrier(b))) break;
     cudaError_t e = cudaMemcpy(all.data(), b->d_case_norms, 8 * all.size(), cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) { rc = b->cuda_fail(e, "norm download"); break; }
@@ -784,11 +890,16 @@ static int run_until(fvs_batch* b, int32_t max_steps, double drop, const double*
     for (int c = 0; c < nc; c++) nact += b->active[c];
     step += n;
     if (nact == 0) break;
-    if (changed) b->plan_dirty = true;
+    trials.after_chunk(n);
+    if (changed) {
+      b->plan_dirty = true;
+      trials.active_changed();
+    }
   }
   cudaEventRecord(b->ev1, b->stream);
   cudaEventSynchronize(b->ev1);
   if (ms) cudaEventElapsedTime(ms, b->ev0, b->ev1);
+  b->tiled = start.tiled; b->fuse = start.fuse; b->block = start.block; b->tile = start.tile; b->bps = start.bps;
   std::fill(b->active.begin(), b->active.end(), 1);
   b->plan_dirty = true;
   if (steps_done) std::memcpy(steps_done, done.data(), 4 * (size_t)nc);
@@ -837,9 +948,7 @@ int fvs_batch_run_to_level_dc(fvs_batch* b, int32_t max_steps, const double* lev
   if (fuse_dc && !b->dp2_mem && !b->arena.alloc(b->dp2_mem, 16 * (size_t)b->nc))
     return b->fail(FVS_ERR_NOMEM, "second tangent buffer");
   b->dc.dP2 = fuse_dc ? static_cast<float*>(b->dp2_mem) : nullptr;
-  const int occ = K.occupancy(b->dc, b->block);
-  if (occ <= 0) return b->fail(FVS_ERR_INVALID, "no resident block for the defect-correction kernel");
-  const int grid = std::max(1, std::min(b->bps, occ)) * b->nsm;
+  if (K.occupancy(b->dc, b->block) <= 0) return b->fail(FVS_ERR_INVALID, "no resident block for the defect-correction kernel");
   const int nc = b->ncases;
   std::vector<double> f(4 * (size_t)nc, -1.0), l(4 * (size_t)nc, 0.0);
   std::vector<int> done(nc, max_steps);
@@ -850,9 +959,13 @@ int fvs_batch_run_to_level_dc(fvs_batch* b, int32_t max_steps, const double* lev
   cudaEventRecord(b->ev0, b->stream);
   int step = 0;
   bool nonfinite = false;
+  ShapeTrials trials(b, true, true);
   while (step < max_steps) {
-    const int n = std::min(chunk, max_steps - step);
+    const int n = trials.before_chunk(std::min(chunk, max_steps - step));
     if (b->plan_dirty && (rc = build_plan(b))) break;
+    const int occ = K.occupancy(b->dc, b->block);
+    if (occ <= 0) { rc = b->fail(FVS_ERR_INVALID, "no resident block for the defect-correction kernel"); break; }
+    const int grid = std::max(1, std::min(b->bps, occ)) * b->nsm;
     // base state of the chunk: fold, FP64 residual and wave speeds, FP32 copies
     K.fold(*d32, b->dc, d64.U, b->stream);
     K64.cvar2pvar(d64, b->stream);
@@ -866,11 +979,14 @@ int fvs_batch_run_to_level_dc(fvs_batch* b, int32_t max_steps, const double* lev
       b->plan.nsteps = 1;
       if (e == cudaSuccess && !b->tgraph_dc)
         e = capture_graph(b, &b->tgraph_dc, [&]() { return K.tiled_step(*d32, b->plan, b->dc, b->block, b->stream); });
+      if (trials.trialling()) cudaEventRecord(b->eva, b->stream);
       for (int i = 0; i < n && e == cudaSuccess; i++) e = cudaGraphLaunch(b->tgraph_dc, b->stream);
     } else {
       b->plan.nsteps = n;
+      if (trials.trialling()) cudaEventRecord(b->eva, b->stream);
       if (e == cudaSuccess) e = K.persistent(*d32, b->plan, b->dc, grid, b->block, b->stream);
     }
+    if (trials.trialling()) cudaEventRecord(b->evb, b->stream);
     if (e != cudaSuccess) { rc = b->cuda_fail(e, "defect-correction chunk"); break; }
     if ((rc = check_barrier(b))) break;
     e = cudaMemcpy(all.data(), b->d_case_norms, 8 * all.size(), cudaMemcpyDeviceToHost);
@@ -902,7 +1018,11 @@ int fvs_batch_run_to_level_dc(fvs_batch* b, int32_t max_steps, const double* lev
     for (int c = 0; c < nc; c++) nact += b->active[c];
     step += n;
     if (nact == 0) break;
-    if (changed) b->plan_dirty = true;
+    trials.after_chunk(n);
+    if (changed) {
+      b->plan_dirty = true;
+      trials.active_changed();
+    }
   }
   // the last correction into the FP64 state
   K.fold(*d32, b->dc, d64.U, b->stream);

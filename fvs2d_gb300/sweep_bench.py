@@ -137,13 +137,14 @@ def run_airfoil(nw=512, nr=256, mach=0.8, aoa=1.25, drop=1e-10, switch=1e-5, max
     return out
 
 
-def profile_batch(ncases=16, steps=400, chunk=200):
+def profile_batch(ncases=16, steps=400, chunk=200, fused=False):
     """A fixed amount of batched work for kernel profiling: the 16-case reduced
-    sweep (261,780 cells), the launch shape the autotuner picks for it (256
-    threads, tiles of 1024, 2 blocks per SM), `steps` mixed persistent steps,
-    then `steps` defect-correction steps, in chunks of `chunk`: one
-    cooperative launch each, steps / chunk launches per phase.  Returns the
-    per-phase seconds."""
+    sweep (261,780 cells), persistent launches of 256 threads, tiles of 1024
+    and 2 blocks per SM, `steps` mixed persistent steps (fused: the fused
+    first-order stage, k_persistent_cell; else separate flux and update
+    phases, k_persistent), then `steps` defect-correction steps, in chunks of
+    `chunk`: one cooperative launch each, steps / chunk launches per phase.
+    Returns the per-phase seconds."""
     from .batch import Batch
     cases = sweep.draw_cases(ncases, 6, (64, 192), (32, 96))
     meshes = [c.mesh() for c in cases]
@@ -151,8 +152,11 @@ def profile_batch(ncases=16, steps=400, chunk=200):
     out = {"cells": int(sum(m.ncells for m in meshes)), "steps": steps, "chunk": chunk}
     with Batch(meshes, [sweep.case_options(c, PREC_MIXED) for c in cases]) as b:
         b.initialize_solution()
+        b.set_mode(False, fused=fused, fixed=True)
         b.set_launch(256, 1024, 2)
-        out["launch"] = {k: v for k, v in b.info().items() if k in ("block", "tile", "blocks_per_sm", "graph")}
+        b.steps(1)
+        out["launch"] = {k: v for k, v in b.info().items() if k in ("block", "tile", "blocks_per_sm", "graph", "fused")}
+        b.initialize_solution()
         t0 = time.perf_counter()
         b.run_to_level(steps, never, chunk)
         t1 = time.perf_counter()
@@ -171,9 +175,10 @@ def main(argv=None):
     ap.add_argument("--epochs", type=int, default=30)
     ap.add_argument("--profile-batch", action="store_true",
                     help="a fixed 16-case batched run (400 mixed + 400 defect-correction steps) for ncu")
+    ap.add_argument("--fused", action="store_true", help="--profile-batch with the fused first-order stage")
     a = ap.parse_args(argv)
     if a.profile_batch:
-        print(json.dumps(profile_batch()), flush=True)
+        print(json.dumps(profile_batch(fused=a.fused)), flush=True)
         return
     print(json.dumps(run(a.n_train, a.n_test, epochs=a.epochs)), flush=True)
 

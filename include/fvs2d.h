@@ -258,10 +258,16 @@ int fvs_batch_set_launch(fvs_batch* b, int32_t block, int32_t tile, int32_t bloc
  * stage, one phase per stage; FVS_BATCH_UNFUSED keeps the separate edge-flux
  * and update phases (the autotuner times both).  FVS_BATCH_DC_FUSED fuses the
  * defect-correction stages the same way (off by default: slower than the
- * separate phases on the measured sweeps). */
+ * separate phases on the measured sweeps).  The run-to-target calls choose
+ * the launch shape again on line as cases converge: once the active cells
+ * fall to half of those at the last choice (and at the start of a
+ * defect-correction run), the next chunks run a few candidate shapes for 20
+ * steps each, timed on the device, and keep the fastest for the rest of the
+ * call; FVS_BATCH_FIXED_SHAPE keeps the set shape throughout. */
 #define FVS_BATCH_TILED 1
 #define FVS_BATCH_UNFUSED 2
 #define FVS_BATCH_DC_FUSED 4
+#define FVS_BATCH_FIXED_SHAPE 8
 int fvs_batch_set_mode(fvs_batch* b, int32_t mode);
 /* switches the arithmetic of all cases (FVS_PREC_*), keeping the FP64
  * state: e.g. MIXED until the FP32 flux floor, then FP64 to a 1e-10 drop */

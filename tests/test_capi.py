@@ -130,3 +130,31 @@ def test_reference_example_inputs(reference_examples):
     assert o.grid_base == "naca0012_omesh" and o.steady and o.lsq_stencil == "nn" and o.ssprk and o.rk_order == 2
     o = read_input(os.path.join(reference_examples, "isentropic_vortex", "fvs2d.input"))
     assert o.vortex and o.grid_base == "vortex" and o.vortex_x == 5.0 and o.vortex_inf[1] == 0.2
+
+
+def test_batch_rejects_invalid_descriptions():
+    """fvs_batch_create checks the batch on the host before any device work:
+    no cases, cases with different schemes, schemes the batched kernels do
+    not run, and a broken mesh in one case (reported with its index)."""
+    from fvs2d_gb300 import meshgen
+    from fvs2d_gb300.batch import Batch
+    from fvs2d_gb300.solver import FvsError
+    lib = capi.load()
+    h = C.c_void_p()
+    assert lib.fvs_batch_create(None, None, 0, 0, C.byref(h)) == capi.FVS_ERR_INVALID
+    assert lib.fvs_batch_last_error(None)
+    m = meshgen.dirichlet_square(6, 6)
+    base = Options(grad_method=3, steady=True, cfl=1.0, rk_nstages=4)
+    bad = [
+        ([m, m], [base, base.replace(cfl=0.5)], capi.FVS_ERR_INVALID, b"share the scheme"),
+        ([m], [base.replace(grad_method=1)], capi.FVS_ERR_INVALID, b"LSQ"),
+        ([m], [base.replace(rk_nstages=2)], capi.FVS_ERR_INVALID, b"stage"),
+    ]
+    broken = meshgen.dirichlet_square(6, 6)
+    broken.tri_nodes[3, 1] = 10**6
+    bad.append(([m, broken], [base, base], capi.FVS_ERR_MESH, b"case 1:"))
+    for meshes, opts, code, words in bad:
+        with pytest.raises(FvsError) as e:
+            Batch(meshes, opts, host_threads=2)
+        assert e.value.code == code, (e.value.code, str(e.value))
+        assert words.decode() in str(e.value), str(e.value)

@@ -163,6 +163,29 @@ def test_fused_first_order_stage_matches_separate_phases(tiled):
         assert not b.info()["fused"]
 
 
+def test_shape_trials_keep_results():
+    """run_to_level tries other launch shapes (fused or not, tiled or not,
+    other tiles) once cases converge; every shape runs the same per-cell
+    arithmetic, so the steps each case takes and its state equal those of a
+    fixed shape.  A converged case stops at the end of its chunk, so both
+    runs use chunks of the trial length (20 steps)."""
+    meshes, opts = sweep(prec=PREC_MIXED, reconst=1, limiter=0)
+    out = []
+    for fixed in (True, False):
+        with Batch(meshes, opts) as b:
+            b.set_mode(False, fixed=fixed)
+            b.initialize_solution()
+            first, _ = b.steps(1)
+            b.initialize_solution()
+            levels = first[:, 0, :] * np.array([1e-1, 1e-2, 1e-3])[:, None]
+            done, _, _, _ = b.run_to_level(20000, levels, chunk=20)
+            assert np.all(done < 20000)
+            out.append((done, [b.get_state(c) for c in range(3)]))
+    assert np.array_equal(out[0][0], out[1][0]), (out[0][0], out[1][0])
+    for c in range(3):
+        assert rel(out[1][1][c], out[0][1][c]) <= 1e-6, (c, rel(out[1][1][c], out[0][1][c]))
+
+
 def test_autotune_keeps_state_and_results():
     meshes, opts = sweep(3)
     with Batch(meshes, opts) as b:
