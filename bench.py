@@ -69,6 +69,64 @@ def dist_env():
     return ws, rank, local
 
 
+class NvmlClocks:
+    """SM clock and clock-event reasons read through NVML every few
+    milliseconds on a background thread during the timed region (read only;
+    nothing is set).  Raises OSError where NVML is not available."""
+
+    # clock-event reason bits of nvml.h
+    REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown", 0x40: "hw_thermal_slowdown"}
+
+    def __init__(self, index: int, period_s: float = 0.005):
+        import ctypes as C
+        import threading
+        lib = C.CDLL("libnvidia-ml.so.1")
+        if lib.nvmlInit_v2() != 0:
+            raise OSError("nvmlInit failed")
+        self.lib, self.C = lib, C
+        self.h = C.c_void_p()
+        if lib.nvmlDeviceGetHandleByIndex_v2(C.c_uint(index), C.byref(self.h)) != 0:
+            raise OSError("no NVML device")
+        self.get_reasons = getattr(lib, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            lib.nvmlDeviceGetCurrentClocksThrottleReasons
+        mx = C.c_uint(0)
+        lib.nvmlDeviceGetMaxClockInfo(self.h, C.c_int(1), C.byref(mx))  # NVML_CLOCK_SM
+        self.max_mhz = float(mx.value)
+        self.sm, self.reasons = [], set()
+        self.period = period_s
+        self.running = True
+        self.t = threading.Thread(target=self._loop, daemon=True)
+        self.t.start()
+
+    def _loop(self):
+        C = self.C
+        clk, rs = C.c_uint(0), C.c_ulonglong(0)
+        while self.running:
+            if self.lib.nvmlDeviceGetClockInfo(self.h, C.c_int(1), C.byref(clk)) == 0:
+                self.sm.append(float(clk.value))
+            if self.get_reasons(self.h, C.byref(rs)) == 0:
+                for bit, name in self.REASONS.items():
+                    if rs.value & bit:
+                        self.reasons.add(name)
+            time.sleep(self.period)
+
+    def stop(self) -> dict:
+        # the loop samples once on entry, so a short region still has a sample
+        self.running = False
+        self.t.join(2.0)
+        self.lib.nvmlShutdown()
+        return {"sm_mhz": statistics.median(self.sm) if self.sm else None, "sm_max_mhz": self.max_mhz,
+                "reasons": sorted(self.reasons), "samples": len(self.sm), "source": "NVML, every 5 ms"}
+
+
+def clock_sampler(index: int):
+    """NVML sampling where the library loads, else nvidia-smi."""
+    try:
+        return NvmlClocks(index)
+    except (OSError, AttributeError):
+        return Clocks(index)
+
+
 class Clocks:
     """nvidia-smi sampling during the timed region."""
 
@@ -199,7 +257,7 @@ def run_ours(args) -> dict:
     # warm-up (also derives dt and captures the step graph)
     s.steps_device(args.warmup)
     barrier()
-    clk = Clocks(int(os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0]) if ws > 1 else 0)
+    clk = clock_sampler(int(os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0]) if ws > 1 else 0)
     ms = s.steps_device(args.steps)
     barrier()
     clocks = clk.stop()
@@ -379,7 +437,7 @@ def main():
     if args.workload in ("sweep", "airfoil", "vortex-period"):
         from fvs2d_gb300 import _build, accuracy, sweep_bench
         _build.build()
-        clk = Clocks(int(os.environ.get("LOCAL_RANK", "0")))
+        clk = clock_sampler(int(os.environ.get("LOCAL_RANK", "0")))
         if args.workload == "vortex-period":
             out = accuracy.run()
         elif args.workload == "sweep":
