@@ -458,8 +458,9 @@ class ShapeTrials {
     if (next_ < 0) return;
     float ms = 0.f;
     cudaEventSynchronize(b_->evb);
-    cudaEventElapsedTime(&ms, b_->eva, b_->evb);
-    us_[next_] = 1000.f * ms / std::max(1, n);
+    const bool ok = cudaEventElapsedTime(&ms, b_->eva, b_->evb) == cudaSuccess;
+    cudaGetLastError();
+    us_[next_] = ok ? 1000.f * ms / std::max(1, n) : 1e30f;
     if (++next_ < (int)cand_.size()) return;
     int best = 0;
     for (int k = 1; k < (int)cand_.size(); k++)
