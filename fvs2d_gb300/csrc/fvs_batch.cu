@@ -433,15 +433,19 @@ class ShapeTrials {
     if (!b->retune) return;
     const LaunchShape cur = {b->tiled, b->fuse, b->block, b->tile, b->bps};
     cand_.push_back(cur);
-    const bool fz = !dc && b->prec == FVS_PREC_MIXED && fusable(b);
-    for (int f = 0; f < (fz ? 2 : 1); f++) {
-      const bool fuse = dc ? b->fuse : f == 1;
-      cand_.push_back({false, fuse, 256, 1024, 2});
-      cand_.push_back({false, fuse, 256, 256, 1});
-      cand_.push_back({false, fuse, 128, 256, 2});
-      cand_.push_back({true, fuse, 256, 1024, 1});
-      cand_.push_back({true, fuse, 128, 256, 1});
-    }
+    // separate phases: large tiles at high occupancy suit large active sets,
+    // short tiles and few blocks small ones
+    const bool sep = dc ? b->fuse : false;
+    for (const LaunchShape& s : {LaunchShape{false, sep, 256, 1024, 2}, LaunchShape{false, sep, 256, 1024, 4},
+                                 LaunchShape{false, sep, 256, 256, 1}, LaunchShape{false, sep, 128, 256, 2},
+                                 LaunchShape{true, sep, 256, 4096, 1}, LaunchShape{true, sep, 256, 1024, 1},
+                                 LaunchShape{true, sep, 128, 256, 1}})
+      cand_.push_back(s);
+    // the fused first-order stage (two blocks of 256 per SM at most)
+    if (!dc && b->prec == FVS_PREC_MIXED && fusable(b))
+      for (const LaunchShape& s : {LaunchShape{false, true, 256, 256, 1}, LaunchShape{false, true, 128, 256, 2},
+                                   LaunchShape{false, true, 256, 1024, 2}, LaunchShape{true, true, 128, 256, 1}})
+        cand_.push_back(s);
     us_.assign(cand_.size(), 0.f);
     cells_ = active_cells();
     if (now) next_ = 0;

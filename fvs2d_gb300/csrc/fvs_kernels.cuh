@@ -1675,7 +1675,7 @@ __device__ __forceinline__ void dc_stage_tile(const DevView& d, const DcView& c,
 }
 
 template <int MODE>
-__global__ void __launch_bounds__(256, 3) k_persistent_dc(const DevView d, const PersistPlan p, const DcView c) {
+__global__ void __launch_bounds__(256, 4) k_persistent_dc(const DevView d, const PersistPlan p, const DcView c) {
   const int nb = gridDim.x;
   const int step0 = *p.step0_dev;
   for (int s = 0; s < p.nsteps; s++) {
