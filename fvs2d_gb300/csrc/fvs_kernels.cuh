@@ -1023,7 +1023,7 @@ __device__ __forceinline__ void case_norms_of_step(const PersistPlan& p, int ste
       double a[4] = {0.0, 0.0, 0.0, 0.0};
       for (int t = ct.y; t < ct.z; t++)
 #pragma unroll
-        for (int k = 0; k < 4; k++) a[k] += p.tile_partials[4 * (size_t)t + k];
+        for (int k = 0; k < 4; k++) a[k] += __ldcg(p.tile_partials + 4 * (size_t)t + k);  // written by other blocks
       double* o = p.case_norms + 4 * ((size_t)ct.x * p.norm_cap + slot);
 #pragma unroll
       for (int k = 0; k < 4; k++) o[k] = sqrt(a[k] / double(ct.w));
