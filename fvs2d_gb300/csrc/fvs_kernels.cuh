@@ -478,6 +478,21 @@ __device__ __forceinline__ void ghost_state(const DevView& d, int rec, double ti
 // values) and no gradient is read.
 enum : int { REC_GENERAL = 0, REC_SPEC = 1, REC_FIRST = 2 };
 
+// Roe flux of one edge slot from its face states, times the face length,
+// into the slot's record; the wave speed times the length likewise
+__device__ __forceinline__ void flux_finish(const DevView& d, int e, const T* pfL, const T* pfR, T2 n, T af) {
+  T flux[4], wsm;
+#if FVS_STRICT
+  roe_flux(T(d.gamma), pfL, pfR, n.x, n.y, flux, wsm);
+#else
+  roe_flux_fast(TP(gamma), TP(gm1), TP(igm1), pfL, pfR, n.x, n.y, flux, wsm);
+#endif
+#pragma unroll
+  for (int v = 0; v < 4; v++) flux[v] = flux[v] * af;
+  st4(static_cast<T*>(d.eflux), e, flux);
+  static_cast<T*>(d.ews)[e] = wsm * af;
+}
+
 template <int REC, bool COH>
 __device__ __forceinline__ void flux_item(const DevView& d, int e, double time) {
   constexpr bool SPEC = REC == REC_SPEC;
@@ -538,16 +553,51 @@ __device__ __forceinline__ void flux_item(const DevView& d, int e, double time) 
     ghost_state(d, d.ebtype[e], time, xy.x, xy.y, n.x, n.y, pfL, pfR);
   }
   }
-  T flux[4], wsm;
-#if FVS_STRICT
-  roe_flux(T(d.gamma), pfL, pfR, n.x, n.y, flux, wsm);
-#else
-  roe_flux_fast(TP(gamma), TP(gm1), TP(igm1), pfL, pfR, n.x, n.y, flux, wsm);
-#endif
+  flux_finish(d, e, pfL, pfR, n, af);
+}
+
+// First-order flux of two edge slots per call (e1 < 0: e0 alone).  The
+// operands of both are loaded before either flux is evaluated, so each thread
+// keeps two chains of dependent loads in flight; the arithmetic is that of
+// flux_item<REC_FIRST>.
+template <bool COH>
+__device__ __forceinline__ void flux_first_pair(const DevView& d, int e0, int e1, double time) {
+  const T* P = static_cast<const T*>(d.Pv);
+  const int e[2] = {e0, e1 >= 0 ? e1 : e0};
+  int2 lr[2];
+  T2 n[2];
+  T af[2], pl[2][4], pr[2][4];
 #pragma unroll
-  for (int v = 0; v < 4; v++) flux[v] = flux[v] * af;
-  st4(static_cast<T*>(d.eflux), e, flux);
-  static_cast<T*>(d.ews)[e] = wsm * af;
+  for (int j = 0; j < 2; j++) {
+    lr[j] = d.ecell[e[j]];
+    n[j] = ld2(d.enrm, e[j]);
+    af[j] = static_cast<const T*>(d.earea)[e[j]];
+  }
+#pragma unroll
+  for (int j = 0; j < 2; j++) {
+    ldc4<COH>(P, lr[j].x, pl[j]);
+    if (lr[j].y >= 0) ldc4<COH>(P, lr[j].y, pr[j]);
+  }
+#pragma unroll
+  for (int j = 0; j < 2; j++) {
+    if (j == 1 && e1 < 0) break;
+    if (lr[j].y < 0) {
+      const T2 xy = ld2(d.exy, e[j]);
+      ghost_state(d, d.ebtype[e[j]], time, xy.x, xy.y, n[j].x, n[j].y, pl[j], pr[j]);
+    }
+    flux_finish(d, e[j], pl[j], pr[j], n[j], af[j]);
+  }
+}
+
+// the edge slots [b, end) of a tile with stride `stride` (the block's
+// threads), first order two at a time
+template <int REC, bool COH>
+__device__ __forceinline__ void flux_range(const DevView& d, int b, int end, int stride, double time) {
+  if (REC == REC_FIRST) {
+    for (int e = b; e < end; e += 2 * stride) flux_first_pair<COH>(d, e, e + stride < end ? e + stride : -1, time);
+  } else {
+    for (int e = b; e < end; e += stride) flux_item<REC, COH>(d, e, time);
+  }
 }
 
 template <int REC>
@@ -1048,7 +1098,7 @@ __global__ void __launch_bounds__(256) k_persistent(const DevView d, const Persi
       }
       for (int t = blockIdx.x; t < p.nedge_tiles; t += nb) {
         const int2 tl = p.edge_tiles[t];
-        for (int e = tl.x + threadIdx.x; e < tl.y; e += blockDim.x) flux_item<REC, true>(d, e, told + sp.dts);
+        flux_range<REC, true>(d, tl.x + threadIdx.x, tl.y, blockDim.x, told + sp.dts);
       }
       if (!grid_sync(p.bar, p.budget)) return;
       for (int t = blockIdx.x; t < p.ncell_tiles; t += nb) {
@@ -1290,7 +1340,7 @@ template <int REC>
 __global__ void __launch_bounds__(256) k_tiles_flux(const DevView d, const PersistPlan p, int stage) {
   const double told = p.t1 + double(*p.step0_dev) * d.dt;
   const int2 tl = p.edge_tiles[blockIdx.x];
-  for (int e = tl.x + threadIdx.x; e < tl.y; e += blockDim.x) flux_item<REC, false>(d, e, told + p.sp[stage].dts);
+  flux_range<REC, false>(d, tl.x + threadIdx.x, tl.y, blockDim.x, told + p.sp[stage].dts);
 }
 
 template <int MODE>
@@ -1481,6 +1531,13 @@ __device__ __forceinline__ void dc_flux_item(const DevView& d, const DcView& c, 
   float f[4];
   dc_edge_jvp(d, c.dP, e, f);
   st4(static_cast<float*>(d.eflux), e, f);
+}
+
+// the edge slots [b, end) of a tile with stride `stride`, one at a time (two
+// per pass, as flux_range does, spilled at this kernel's register budget and
+// ran slower)
+__device__ __forceinline__ void dc_flux_range(const DevView& d, const DcView& c, int b, int end, int stride) {
+  for (int e = b; e < end; e += stride) dc_flux_item(d, c, e);
 }
 
 // One cell of an RK stage of the correction with the residual R0 + J dU (the
@@ -1682,7 +1739,7 @@ __global__ void __launch_bounds__(256, 4) k_persistent_dc(const DevView d, const
     for (int k = 0; k < p.nstages; k++) {
       for (int t = blockIdx.x; t < p.nedge_tiles; t += nb) {
         const int2 tl = p.edge_tiles[t];
-        for (int e = tl.x + threadIdx.x; e < tl.y; e += blockDim.x) dc_flux_item(d, c, e);
+        dc_flux_range(d, c, tl.x + threadIdx.x, tl.y, blockDim.x);
       }
       if (!grid_sync(p.bar, p.budget)) return;
       for (int t = blockIdx.x; t < p.ncell_tiles; t += nb) dc_stage_tile<MODE, false>(d, c, p, k, t);
@@ -1773,7 +1830,7 @@ static cudaError_t dc_persistent(const DevView& d, const PersistPlan& p, const D
 // one defect-correction step as tile launches (for graph capture)
 __global__ void __launch_bounds__(256) k_tiles_dc_flux(const DevView d, const DcView c, const PersistPlan p) {
   const int2 tl = p.edge_tiles[blockIdx.x];
-  for (int e = tl.x + threadIdx.x; e < tl.y; e += blockDim.x) dc_flux_item(d, c, e);
+  dc_flux_range(d, c, tl.x + threadIdx.x, tl.y, blockDim.x);
 }
 
 template <int MODE, bool FUSED>
