@@ -1,8 +1,9 @@
 """Batched independent cases through the C-ABI (fvs_batch_*).
 
 All cases share the scheme; each has its own mesh, Mach number and angle of
-attack.  One cooperative persistent kernel advances every active case per
-chunk of steps; converged cases leave the work lists.
+attack.  One launch advances every active case per chunk of steps (a
+cooperative persistent kernel, or a CUDA graph of tile launches per step);
+converged cases leave the work lists.
 """
 from __future__ import annotations
 

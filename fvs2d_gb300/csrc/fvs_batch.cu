@@ -1,15 +1,21 @@
-// fvs_batch.cu — many independent cases in one persistent launch.
+// fvs_batch.cu — many independent cases in one launch.
 //
 // The cases' meshes are packed as a disjoint union (each case's cells and
 // edge slots contiguous, fvs_layout.hpp), so the per-item device code of the
 // single-mesh path serves unchanged; what is per case is the free stream
 // (boundary records carry the case index), the residual norm (cell tiles
 // never straddle cases) and convergence (converged cases are dropped from
-// the tile lists).  One cooperative launch of k_persistent advances all
-// active cases by a chunk of RK steps with bounded grid barriers between the
-// phases; the launch is captured once in a CUDA graph and replayed.  The
-// launch shape (block size, tile length, resident blocks per SM) comes from
-// a small autotuner that times the candidates on the batch itself.
+// the tile lists).  Launch forms:
+//  - one cooperative launch of k_persistent advances all active cases by a
+//    chunk of RK steps, with bounded grid barriers between the phases,
+//    captured once in a CUDA graph and replayed;
+//  - a CUDA graph of one step's tile launches (one block per tile and
+//    phase), replayed once per step;
+//  - for first-order mixed batches, either form with the fused stage (each
+//    cell evaluates its own faces' fluxes: one phase per stage).
+// The launch shape (form, block size, tile length, resident blocks per SM)
+// comes from an autotuner that times the candidates on the batch itself,
+// and the run-to-target calls try shapes again as the active set shrinks.
 //
 // The reference runs one case per process (src/fvs2d.f90); the batch has no
 // counterpart there beyond running time_integration on each case.
