@@ -99,7 +99,10 @@ inline std::vector<int> rcm_order(const HostMesh& h) {
         int n = h.nghbr[4 * c + k];
         if (n >= 0 && !seen[n]) nb[m++] = n;
       }
-      std::sort(nb, nb + m, [&](int a, int b) { return deg[a] != deg[b] ? deg[a] < deg[b] : a < b; });
+      // at most 4 neighbours: insertion sort by (degree, index), a total order
+      for (int i = 1; i < m; i++)
+        for (int j = i; j > 0 && (deg[nb[j]] != deg[nb[j - 1]] ? deg[nb[j]] < deg[nb[j - 1]] : nb[j] < nb[j - 1]); j--)
+          std::swap(nb[j], nb[j - 1]);
       for (int i = 0; i < m; i++) {
         seen[nb[i]] = 1;
         order.push_back(nb[i]);
