@@ -172,3 +172,43 @@ def test_errors_match_oracle(case, code):
     with pytest.raises(Exception) as e:
         Oracle(mesh, opt)
     assert getattr(e.value, "code", None) == code
+
+
+@pytest.mark.parametrize("case,code", [
+    ("no_cells", capi.FVS_ERR_INVALID),
+    ("no_boundary_list", capi.FVS_ERR_MESH),
+    ("degenerate_triangle", capi.FVS_ERR_MESH),
+    ("clockwise_triangle", capi.FVS_ERR_MESH),
+    ("duplicate_cell", capi.FVS_ERR_MESH),
+    ("unused_node", capi.FVS_OK),
+])
+def test_edge_case_meshes_match_oracle(case, code):
+    """Empty and malformed meshes: the library's setup and the oracle give the
+    same verdict, and an unused node (allowed by the reference's reader) sets
+    up as usual."""
+    import copy
+    mesh = copy.deepcopy(meshgen.dirichlet_square(6, 6))
+    if case == "no_cells":
+        mesh.tri_nodes = np.zeros((0, 3), np.int32)
+        mesh.bndry_cells = [np.zeros(0, np.int32)]
+    elif case == "no_boundary_list":
+        mesh.bndry_types, mesh.bndry_cells = [], []
+    elif case == "degenerate_triangle":
+        mesh.tri_nodes[0, 1] = mesh.tri_nodes[0, 0]
+    elif case == "clockwise_triangle":
+        mesh.tri_nodes[0] = mesh.tri_nodes[0][::-1]
+    elif case == "duplicate_cell":
+        mesh.tri_nodes[5] = mesh.tri_nodes[4]
+    elif case == "unused_node":
+        mesh.node_xy = np.concatenate([mesh.node_xy, [[100.0, 100.0]]])
+    hh = HostHandle(mesh, Options())
+    try:
+        assert hh.rc == code, hh.msg
+    finally:
+        hh.close()
+    if code == capi.FVS_OK:
+        Oracle(mesh, Options()).close()
+    else:
+        with pytest.raises(Exception) as e:
+            Oracle(mesh, Options())
+        assert getattr(e.value, "code", None) == code
