@@ -1,0 +1,59 @@
+"""Committed golden fixtures (tests/golden/*.npz, written by
+tests/golden/make_golden.py from the CPU oracle).
+
+On the CPU the oracle must still reproduce them bit for bit: this pins the
+restatement against later edits.  On the GPU the strict FP64 path must meet
+them bit for bit from the stored start state (states, residuals, wave-speed
+sums; the norms are reduced in another order, rtol 1e-13), and the FP64 path
+with FMA contraction within 1e-12 of max|value|."""
+import os
+
+import numpy as np
+import pytest
+
+from fvs2d_gb300 import PREC_FP64, PREC_FP64_STRICT, Solver
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+import sys  # noqa: E402
+
+sys.path.insert(0, os.path.join(HERE, "golden"))
+from make_golden import STEPS, compute, golden_cases  # noqa: E402
+
+CASES = golden_cases()
+
+
+def fixture(name):
+    with np.load(os.path.join(HERE, "golden", name + ".npz")) as z:
+        return {k: z[k] for k in z.files}
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_oracle_reproduces_fixture(name):
+    mesh, opt = CASES[name]
+    want = fixture(name)
+    got = compute(mesh, opt)
+    for k in ("start", "norms", "state", "resid", "ws"):
+        assert np.array_equal(got[k], want[k]), (name, k)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("prec", [PREC_FP64_STRICT, PREC_FP64])
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_gpu_meets_fixture(name, prec):
+    mesh, opt = CASES[name]
+    want = fixture(name)
+    with Solver(mesh, opt.replace(precision=prec)) as s:
+        s.initialize_solution()
+        s.cvar = want["start"]
+        norms = s.time_integration(0.0, STEPS)
+        state = s.cvar
+        resid, ws = s.compute_residual(float(want["t_end"]))
+    if prec == PREC_FP64_STRICT:
+        assert np.array_equal(state, want["state"]), (name, float(np.abs(state - want["state"]).max()))
+        assert np.array_equal(resid, want["resid"]), name
+        assert np.array_equal(ws, want["ws"]), name
+        assert np.allclose(norms, want["norms"], rtol=1e-13, atol=0)
+    else:
+        for got, ref in ((state, want["state"]), (resid, want["resid"]), (ws, want["ws"])):
+            assert float(np.abs(got - ref).max() / np.abs(ref).max()) <= 1e-12, name
+        assert np.allclose(norms, want["norms"], rtol=1e-9, atol=0)
