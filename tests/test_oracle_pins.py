@@ -128,3 +128,54 @@ def test_invalid_options_rejected(bad):
     with pytest.raises(OracleError) as e:
         Oracle(meshgen.dirichlet_square(4, 4), Options(**bad))
     assert e.value.code == 1
+
+
+@pytest.mark.parametrize("grad_method,limiter", [(3, 0), (3, 1), (1, 0), (2, 0)])
+def test_free_stream_preserved(grad_method, limiter):
+    """Property of the reference's scheme: a uniform state on a closed
+    (periodic) mesh has a zero residual up to rounding, with every gradient
+    (the faces' normals times lengths of each cell sum to zero)."""
+    mesh = meshgen.periodic_square(16, 12, jitter=0.25)
+    o = Oracle(mesh, Options(vortex=False, mach_inf=0.6, aoa_inf_deg=20.0, grad_method=grad_method,
+                             limiter=limiter, dt=0.01))
+    o.initialize_solution()
+    u = o.cvar
+    assert np.ptp(u, axis=0).max() == 0.0  # a uniform free stream
+    r, _ = o.compute_residual(0.0)
+    o.close()
+    h = 10.0 / 16
+    # flux magnitudes are O(1); R = -sum(F.n A)/vol ~ 1/h per unbalanced face
+    assert np.abs(r).max() <= 1e-12 / h, np.abs(r).max()
+
+
+def test_discrete_conservation_periodic():
+    """Each interior face's flux leaves one cell and enters the other, so on a
+    periodic mesh sum(vol * resid) vanishes to rounding for any state."""
+    mesh, opt = cases.periodic_vortex(16, jitter=0.2)
+    o = Oracle(mesh, opt)
+    o.initialize_solution()
+    r, _ = o.compute_residual(0.0)
+    vol = mesh_volumes(mesh)
+    total = (vol[:, None] * r).sum(axis=0)
+    scale = (vol[:, None] * np.abs(r)).sum(axis=0)
+    o.close()
+    assert np.all(np.abs(total) <= 1e-13 * scale), (total, scale)
+
+
+def mesh_volumes(mesh):
+    """Cell areas from the node coordinates (shoelace), minimum-image across
+    the periods, in reference cell order (triangles, then quadrilaterals)."""
+    xy = mesh.node_xy
+    out = []
+    for cells in (mesh.tri_nodes, mesh.quad_nodes):
+        if cells.shape[0] == 0:
+            continue
+        p = xy[cells - 1]  # (n, k, 2)
+        d = p - p[:, :1, :]
+        if mesh.period_x > 0:
+            d[..., 0] -= mesh.period_x * np.round(d[..., 0] / mesh.period_x)
+        if mesh.period_y > 0:
+            d[..., 1] -= mesh.period_y * np.round(d[..., 1] / mesh.period_y)
+        x, y = d[..., 0], d[..., 1]
+        out.append(0.5 * (x * np.roll(y, -1, axis=1) - np.roll(x, -1, axis=1) * y).sum(axis=1))
+    return np.concatenate(out)
