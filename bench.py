@@ -358,12 +358,17 @@ def host_threads() -> int:
         return os.cpu_count() or 1
 
 
+def oracle_build(orc) -> str:
+    return ("built -O3 -ffast-math like the reference's -Ofast" if orc.timed
+            else "built -O2 -ffp-contract=off (the -O3 -ffast-math build was unavailable)")
+
+
 def cpu_baseline(mesh, opt, budget_s: float = 12.0, nthreads: int | None = None) -> dict:
     """The oracle on the host cores: a bounded number of full-mesh steps."""
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     from oracle_lib import Oracle
     nthreads = nthreads or host_threads()
-    orc = Oracle(mesh, opt, nthreads=nthreads)
+    orc = Oracle(mesh, opt, nthreads=nthreads, timed=True)
     orc.initialize_solution()
     t0 = time.perf_counter()
     orc.time_integration(0.0, 1)
@@ -375,7 +380,7 @@ def cpu_baseline(mesh, opt, budget_s: float = 12.0, nthreads: int | None = None)
     nst = orc.sizes.nstages
     return {"value": orc.ncells * nst * k / t, "unit": METRIC, "cores": nthreads, "kind": "port",
             "sample": f"{k} full SSP-RK3 steps of the {orc.ncells}-cell mesh (after 1 untimed step), "
-                      f"race-free OpenMP oracle with {nthreads} threads",
+                      f"race-free OpenMP oracle with {nthreads} threads, {oracle_build(orc)}",
             "seconds": round(t, 3)}
 
 
@@ -388,7 +393,7 @@ def run_reference(args) -> dict | None:
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     from oracle_lib import Oracle
     nth = host_threads()
-    orc = Oracle(mesh, opt, nthreads=nth)
+    orc = Oracle(mesh, opt, nthreads=nth, timed=True)
     orc.initialize_solution()
     for _ in range(max(1, min(args.warmup, 1))):
         orc.time_integration(0.0, 1)
@@ -404,7 +409,7 @@ def run_reference(args) -> dict | None:
     nc, nst = orc.ncells, orc.sizes.nstages
     v = nc * nst * k / t
     sample = (f"{k} full SSP-RK3 steps of the {nc}-cell mesh on {nth} host threads (race-free OpenMP restatement "
-              f"of the Fortran reference; the reference itself needs a Fortran compiler and MPI)")
+              f"of the Fortran reference, {oracle_build(orc)}; the reference itself needs a Fortran compiler and MPI)")
     return {"metric": METRIC, "value": v, "unit": METRIC, "n_gpus": ws, "steps": k, "warmup": args.warmup,
             "ms_per_step": t * 1e3 / k, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded mesh generator, analytic vortex initial state)",

@@ -79,3 +79,30 @@ def test_reference_arm_runs_on_rank_zero_only(monkeypatch):
     monkeypatch.setenv("LOCAL_RANK", "1")
     args = argparse.Namespace(steps=1, warmup=1)
     assert bench.run_reference(args) is None
+
+
+def test_timed_oracle_falls_back_to_the_checker_build(monkeypatch):
+    """The CPU baseline runs the -O3 -ffast-math oracle build; where that
+    build fails it runs the checker's -O2 build and says so."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import cases
+    import oracle_lib  # puts oracle/ on the path
+
+    import bench
+    import build_oracle
+    real = build_oracle.build
+
+    def no_timed(force=False, timed=False):
+        if timed:
+            raise RuntimeError("timed build unavailable")
+        return real(force=force)
+
+    monkeypatch.setattr(build_oracle, "build", no_timed)
+    monkeypatch.setattr(oracle_lib, "_LIBS", {})
+    mesh, opt = cases.airfoil(24, 8)
+    orc = oracle_lib.Oracle(mesh, opt, timed=True)
+    try:
+        assert orc.timed is False
+        assert "-O2" in bench.oracle_build(orc)
+    finally:
+        orc.close()
