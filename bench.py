@@ -16,6 +16,9 @@ all cells; the metric is cell-stage updates/s = ncells * 3 * steps / time.
   roofline  dominant kernel: algorithmic bytes per launch / mean launch time
   cpu_baseline  the CPU oracle (a restatement of the Fortran reference) on
             the host cores, on a bounded sample of the same workload
+  time_to_drop  wall time to a 1e-10 residual drop on the 261,120-cell
+            NACA0012 O-grid: plain FP64 solver against the batched precision
+            ladder (rank 0 only)
 
 --impl reference times the reference's CPU algorithm (the oracle port: the
 Fortran reference cannot be built without a Fortran compiler and MPI) on all
@@ -328,9 +331,24 @@ def run_ours(args) -> dict:
     if rank == 0 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(mesh, opt, budget_s=args.cpu_budget)
     s.close()
+    if rank == 0 and args.time_to_drop:
+        out["time_to_drop"] = time_to_drop()
     if ws > 1:
         tdist.destroy_process_group()
     return out if rank == 0 else None
+
+
+def time_to_drop() -> dict:
+    """The second half of the headline metric: wall time to a 1e-10 drop of
+    every RMS(dU) component on the 261,120-cell NACA0012 O-grid (M 0.8,
+    1.25 deg, steady SSP-RK(4,2), local dt at CFL 1.25), the plain FP64
+    solver against the batched precision ladder (mixed, then defect
+    correction, then an FP64 check), with its own clock record."""
+    from fvs2d_gb300 import sweep_bench
+    clk = clock_sampler(0)
+    r = sweep_bench.run_airfoil()
+    r["clocks"] = clk.stop()
+    return r
 
 
 def max_over_ranks(seconds: float, device: str) -> float:
@@ -428,6 +446,8 @@ def main():
     ap.add_argument("--no-variants", dest="variants", action="store_false")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=12.0)
+    ap.add_argument("--no-time-to-drop", dest="time_to_drop", action="store_false",
+                    help="skip the time-to-1e-10-drop measurement on the NACA0012 O-grid (about 45 s)")
     ap.add_argument("--workload", default="vortex", choices=["vortex", "sweep", "airfoil", "vortex-period"],
                     help="vortex: the 1,048,576-cell throughput case (default); sweep: time to a 1e-10 drop on an "
                          "airfoil sweep, plain FP64 vs batched ladder vs learned warm start; airfoil: time to a "

@@ -547,6 +547,7 @@ extern "C" {
 
 int fvs_batch_create(const fvs_mesh* meshes, const fvs_options* opts, int32_t ncases, int32_t host_threads,
                      fvs_batch** out) {
+  NvtxRange nv("fvs batch setup");
   if (!out) return FVS_ERR_INVALID;
   *out = nullptr;
   if (!meshes || !opts || ncases <= 0) {
@@ -763,6 +764,7 @@ int fvs_batch_set_launch(fvs_batch* b, int32_t block, int32_t tile, int32_t bloc
 
 // nsteps steps of every active case; norms (optional) [ncases][nsteps][4]
 int fvs_batch_steps(fvs_batch* b, int32_t nsteps, double* norms, float* ms) {
+  NvtxRange nv("fvs batch steps");
   if (!b || nsteps <= 0 || nsteps > b->norm_cap) return FVS_ERR_INVALID;
   cudaEventRecord(b->ev0, b->stream);
   int rc = launch_chunk(b, nsteps, 0);
@@ -782,6 +784,7 @@ int fvs_batch_steps(fvs_batch* b, int32_t nsteps, double* norms, float* ms) {
 
 // Candidate launch shapes timed on the batch itself; the state is restored.
 int fvs_batch_autotune(fvs_batch* b, int32_t trial_steps, float* best_ms) {
+  NvtxRange nv("fvs batch autotune");
   if (!b || trial_steps <= 0 || trial_steps > b->norm_cap) return FVS_ERR_INVALID;
   cudaError_t e = cudaMemcpy(b->d_backup, b->d.U, 32 * (size_t)b->nc, cudaMemcpyDeviceToDevice);
   if (e != cudaSuccess) return b->cuda_fail(e, "state backup");
@@ -928,6 +931,7 @@ static int run_until(fvs_batch* b, int32_t max_steps, double drop, const double*
 // batch in FP64 with the folded state.
 int fvs_batch_run_to_level_dc(fvs_batch* b, int32_t max_steps, const double* levels, int32_t chunk,
                               int32_t* steps_done, double* first, double* last, float* ms) {
+  NvtxRange nv("fvs batch defect correction");
   if (!b || !levels || max_steps <= 0 || chunk <= 0 || chunk > b->norm_cap) return FVS_ERR_INVALID;
   if (!b->base.steady || b->base.reconst != FVS_RECON_UPWIND1)
     return b->fail(FVS_ERR_INVALID, "defect correction runs first-order steady batches");
@@ -1059,6 +1063,7 @@ int fvs_batch_run_to_drop(fvs_batch* b, int32_t max_steps, double drop, int32_t 
 
 int fvs_batch_run_to_level(fvs_batch* b, int32_t max_steps, const double* levels, int32_t chunk, int32_t* steps_done,
                            double* first, double* last, float* ms) {
+  NvtxRange nv("fvs batch run to level");
   if (!levels) return FVS_ERR_INVALID;
   return run_until(b, max_steps, 0.0, levels, chunk, steps_done, first, last, ms);
 }

@@ -239,6 +239,7 @@ int check_launch(fvs_handle* H, const char* where) {
 
 // residual of the current device state at `time` (stage-free): fills d.resid, d.ws
 int device_residual(fvs_handle* H, double time) {
+  NvtxRange nv("fvs residual (gradient, flux, gather)");
   H->h_small[0] = time;
   cudaError_t e = cudaMemcpyAsync(H->d.tctl + 1, H->h_small, sizeof(double), cudaMemcpyHostToDevice, H->stream);
   if (e != cudaSuccess) return H->cuda_fail(e, "time upload");
@@ -272,6 +273,7 @@ int ensure_dt(fvs_handle* H, double t1) {
 }
 
 int state_in(fvs_handle* H, const double* cvar) {
+  NvtxRange nv("fvs state upload");
   const size_t bytes = 32 * (size_t)H->hm.nc;
   cudaError_t e = cudaMemcpyAsync(H->d_stage, cvar, bytes, cudaMemcpyHostToDevice, H->stream);
   if (e != cudaSuccess) return H->cuda_fail(e, "state upload");
@@ -281,6 +283,7 @@ int state_in(fvs_handle* H, const double* cvar) {
 }
 
 int state_out(fvs_handle* H, const double* dev, double* host, int width) {
+  NvtxRange nv("fvs state download");
   const int nc = H->hm.nc;
   k_gather_out<<<(nc + 255) / 256, 256, 0, H->stream>>>(dev, H->d_perm, H->d_stage, nc, width);
   cudaError_t e = cudaMemcpyAsync(host, H->d_stage, sizeof(double) * width * (size_t)nc, cudaMemcpyDeviceToHost, H->stream);
@@ -351,7 +354,10 @@ int fvs_create(const fvs_mesh* mesh, const fvs_options* opt, fvs_handle** out) {
   std::unique_ptr<fvs_handle> H(new fvs_handle());
   H->o = *opt;
   if (H->o.reconst != FVS_RECON_UMUSCL) H->o.umuscl = 0.0;  // src/input.f90:250,254
-  rc = build_host_mesh(mesh, &H->o, H->hm, err);
+  {
+    NvtxRange nv("fvs host setup (grid_data, stencils)");
+    rc = build_host_mesh(mesh, &H->o, H->hm, err);
+  }
   if (rc) { g_create_error = err; return rc; }
   // free stream, src/data_solution.f90:55-63
   const double aoa = H->o.aoa_inf_deg * 3.141592653589793238462643383279502884 / 180.0;
@@ -384,7 +390,10 @@ int fvs_create(const fvs_mesh* mesh, const fvs_options* opt, fvs_handle** out) {
   d.vx = H->o.vortex_x; d.vy = H->o.vortex_y; d.vkappa = H->o.vortex_kappa;
   for (int k = 0; k < 4; k++) { d.vinf[k] = H->o.vortex_inf[k]; d.pinf[k] = H->pvar_inf[k]; }
   mms_constants(d.mc);
-  rc = H->mixed ? build_device<float>(H.get()) : H->df ? build_device<df64>(H.get()) : build_device<double>(H.get());
+  {
+    NvtxRange nv("fvs device layout and upload");
+    rc = H->mixed ? build_device<float>(H.get()) : H->df ? build_device<df64>(H.get()) : build_device<double>(H.get());
+  }
   if (rc) { g_create_error = H->err; return rc; }
   H->dt = H->o.dt;
   // steady runs start from dt_local = dt (src/runge_kutta.f90:73-76)
@@ -530,6 +539,7 @@ int fvs_get_gradient(fvs_handle* h, double* grad, double* phi) {
 }
 
 static int run_steps(fvs_handle* h, double t1, int nsteps, double* resnorm, float* ms) {
+  NvtxRange nv("fvs time integration (graph replays)");
   int rc = ensure_dt(h, t1);
   if (rc) return rc;
   if ((rc = ensure_graph(h, 1))) return rc;
@@ -564,9 +574,20 @@ static int run_steps(fvs_handle* h, double t1, int nsteps, double* resnorm, floa
   }
   e = cudaStreamSynchronize(h->stream);
   if (e != cudaSuccess) return h->cuda_fail(e, "time integration");
-  if (resnorm)
+  if (resnorm) {
     for (size_t i = 0; i < 4 * (size_t)nsteps; i++)
       if (!std::isfinite(resnorm[i])) return h->fail(FVS_ERR_NONFINITE, "residual norm is not finite at step " + std::to_string(i / 4 + 1));
+  } else {
+    // no norms requested (device-resident stepping): the last step's norms
+    // from the device ring; a non-finite state stays non-finite, so the last
+    // step shows whether any step went bad
+    double last[4];
+    e = cudaMemcpy(last, h->d.norms + 4 * (size_t)((nsteps - 1) % cap), sizeof last, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return h->cuda_fail(e, "norm download");
+    for (int k = 0; k < 4; k++)
+      if (!std::isfinite(last[k]))
+        return h->fail(FVS_ERR_NONFINITE, "residual norm is not finite after step " + std::to_string(nsteps));
+  }
   return FVS_OK;
 }
 
@@ -638,6 +659,7 @@ int fvs_vortex_error(fvs_handle* h, double time, double* e) {
 }
 
 int fvs_wall_loads(fvs_handle* h, int32_t ib, double* edge_out, double* loads) {
+  NvtxRange nv("fvs wall loads");
   if (h && h->host_only) return h->fail(FVS_ERR_INVALID, "host-only handle (fvs_create_host) has no device state");
   if (!h || !loads) return FVS_ERR_INVALID;
   const HostMesh& m = h->hm;

@@ -3,6 +3,7 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <cstdint>
 #include <string>
@@ -11,6 +12,15 @@
 #include "../../include/fvs2d.h"
 
 namespace fvs {
+
+// NVTX range over a host-side phase (setup, upload, stepping, download):
+// visible in a profiler's timeline, free when no tool is attached
+struct NvtxRange {
+  explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+  NvtxRange(const NvtxRange&) = delete;
+  NvtxRange& operator=(const NvtxRange&) = delete;
+};
 
 // ---------------------------------------------------------------------------
 // Host mesh in the reference's numbering, 0-based, "-1" where the reference

@@ -22,7 +22,9 @@
 //    threads without ordering) race on the array.
 //  - the first call on a device, with that device current, looks up the
 //    array's device address (cudaGetSymbolAddress); make that first call
-//    before any stream capture.
+//    before any stream capture.  The address is kept for the life of the
+//    process, so a cudaDeviceReset after the first call is not supported
+//    (the kept address would point into the destroyed context).
 #include <cuda_runtime.h>
 
 #include <mutex>

@@ -8,7 +8,8 @@
  * reading the mesh of src/data_grid.f90:23-68, the solution arrays of
  * src/data_solution.f90:16-28 and the scheme flags of src/input.f90:9-56.
  * The entry points below replace those procedures one-for-one.  A Fortran
- * host binds them through ISO_C_BINDING (interface block in INTEGRATION.md).
+ * host binds them through an ISO_C_BINDING interface block that declares
+ * each prototype below with bind(C) and value/reference arguments to match.
  *
  * Conventions
  *  - All arrays are caller-owned host memory unless a name says "device".
@@ -334,8 +335,11 @@ int fvs_mlp_predict(fvs_mlp* m, const float* x, int64_t n, float* y);
  * GPU that loads the library, held until exit), so ncells is limited to
  * FVS_NOALLOC_MAX_CELLS; larger inputs return FVS_ERR_INVALID.  Every call on
  * a device shares that array: calls that overlap on the GPU race.  The first
- * call on a device (with that device current) looks up the array's address;
- * make it before any stream capture.  The call is asynchronous on `stream`. */
+ * call on a device (with that device current) looks up the array's address
+ * and keeps it for the life of the process; make it before any stream
+ * capture.  A cudaDeviceReset after that first call is not supported: the
+ * kept address would then point into the destroyed context.  The call is
+ * asynchronous on `stream`. */
 #define FVS_NOALLOC_MAX_BLOCKS 8192
 #define FVS_NOALLOC_MAX_CELLS (FVS_NOALLOC_MAX_BLOCKS * 256)
 int fvs_rms_delta_noalloc(const double* dev_u, const double* dev_u0, int32_t ncells, double* dev_norm4, void* stream);

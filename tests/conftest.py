@@ -7,7 +7,9 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 sys.path.insert(0, ROOT)
 sys.path.insert(0, os.path.join(ROOT, "tests"))
 
-REFERENCE = "/root/reference"
+# mount point of the reference sources (read only); tests that need them skip
+# where it is absent
+REFERENCE = os.environ.get("FVS2D_REFERENCE", "/root/reference")
 
 
 def pytest_configure(config):

@@ -7,7 +7,8 @@ oracle must still reproduce them bit for bit: this pins the restatement
 against later edits.  On the GPU the strict FP64 path must meet
 them bit for bit from the stored start state (states, residuals, wave-speed
 sums; the norms are reduced in another order, rtol 1e-13), and the FP64 path
-with FMA contraction within 1e-12 of max|value| (1e-11 with the limiter)."""
+with FMA contraction within 1e-12 of max|value| per step (over the 12 steps:
+1e-12 without the limiter, 12 x 1e-12 with it)."""
 import os
 
 import numpy as np
@@ -56,9 +57,12 @@ def test_gpu_meets_fixture(name, prec):
         assert np.array_equal(ws, want["ws"]), name
         assert np.allclose(norms, want["norms"], rtol=1e-13, atol=0)
     else:
-        # the limiter's min/max selections amplify the contraction's rounding
-        # differences: 1.7e-12 measured on the limited transonic airfoil
-        tol = 1e-11 if opt.limiter else 1e-12
+        # The bar is 1e-12 of max|value| per step.  Unlimited cases meet it
+        # over all STEPS steps at once.  With the limiter, its min/max
+        # selections amplify the contraction's rounding differences, so the
+        # bar accumulates over the steps: STEPS * 1e-12 = 1.2e-11 after 12
+        # steps (1.7e-12 measured on the limited transonic airfoil).
+        tol = STEPS * 1e-12 if opt.limiter else 1e-12
         for key, got, ref in (("state", state, want["state"]), ("resid", resid, want["resid"]), ("ws", ws, want["ws"])):
             assert float(np.abs(got - ref).max() / np.abs(ref).max()) <= tol, (name, key)
         assert np.allclose(norms, want["norms"], rtol=1e-9, atol=0)

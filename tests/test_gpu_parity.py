@@ -203,6 +203,35 @@ def test_nonfinite_detected():
         assert e.value.code == capi.FVS_ERR_NONFINITE
 
 
+def test_nonfinite_detected_without_norm_log():
+    """fvs_steps_device asks for no norms; the non-finite state is still
+    reported (from the last step's norms on the device)."""
+    mesh, opt = cases.periodic_vortex(12)
+    with Solver(mesh, opt) as s:
+        s.initialize_solution()
+        u = s.cvar
+        u[7, 2] = np.nan
+        s.cvar = u
+        with pytest.raises(FvsError) as e:
+            s.steps_device(3)
+        assert e.value.code == capi.FVS_ERR_NONFINITE
+
+
+def test_divergence_detected():
+    """A time step above the scheme's stability limit: the RMS(dU) of the
+    oracle's run (CPU) grows 1.27, 1.70, 2.52, 3.45, 5.38 x the first step's
+    and turns non-finite at step 7.  With diverge_factor 2 and a check every
+    step, the device run stops with FVS_ERR_DIVERGED at step 4, before any
+    value becomes non-finite."""
+    mesh, opt = cases.periodic_vortex(24, jitter=0.2, cfl=2.0, diverge_factor=2.0)
+    with Solver(mesh, opt) as s:
+        s.initialize_solution()
+        with pytest.raises(FvsError) as e:
+            s.run_to_drop(0.0, 50, drop=1e-10, check_every=1)
+        assert e.value.code == capi.FVS_ERR_DIVERGED
+        assert np.all(np.isfinite(s.cvar))
+
+
 def test_run_to_drop_matches_step_log():
     # CFL 0.5: the second-order limited scheme diverges above ~0.8 on this mesh
     mesh, opt = cases.airfoil(nw=64, nr=24, cfl=0.5)

@@ -44,6 +44,32 @@ def test_noalloc_norm_matches_time_integration_log():
             # same tolerance as the other norm checks (blocked reductions in a
             # different cell order)
             assert np.allclose(got, ref, rtol=1e-13, atol=0), (call, got, ref)
+        # a prefix that ends inside a block of 256 cells (the partial last
+        # block), on a stream other than the default one, against numpy
+        m = n - 37
+        side = torch.cuda.Stream()
+        with torch.cuda.stream(side):
+            out.fill_(-1.0)
+            rc = lib.fvs_rms_delta_noalloc(C.c_void_p(du1.data_ptr()), C.c_void_p(du0.data_ptr()), m,
+                                           C.c_void_p(out.data_ptr()), C.c_void_p(side.cuda_stream))
+            assert rc == capi.FVS_OK, f"prefix call: rc {rc}"
+        side.synchronize()
+        got = out.cpu().numpy()
+        ref = np.sqrt(np.mean((u1[:m] - u0[:m]) ** 2, axis=0))
+        assert np.allclose(got, ref, rtol=1e-13, atol=0), (got, ref)
+        # exactly the accepted maximum (every block of the fixed array in use)
+        cap = 2_097_152
+        g = torch.Generator(device="cuda").manual_seed(3)
+        a = torch.rand((cap, 4), dtype=torch.float64, device="cuda", generator=g)
+        b = torch.rand((cap, 4), dtype=torch.float64, device="cuda", generator=g)
+        out.fill_(-1.0)
+        torch.cuda.synchronize()
+        assert lib.fvs_rms_delta_noalloc(C.c_void_p(a.data_ptr()), C.c_void_p(b.data_ptr()), cap,
+                                         C.c_void_p(out.data_ptr()), None) == capi.FVS_OK
+        torch.cuda.synchronize()
+        ref = np.sqrt(np.mean((a.cpu().numpy() - b.cpu().numpy()) ** 2, axis=0))
+        assert np.allclose(out.cpu().numpy(), ref, rtol=1e-13, atol=0)
+        del a, b
         # beyond the fixed scratch: rejected before any device work
         big = 2_097_152 + 1
         assert lib.fvs_rms_delta_noalloc(C.c_void_p(du1.data_ptr()), C.c_void_p(du0.data_ptr()), big,
