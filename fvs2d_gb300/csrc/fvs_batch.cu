@@ -213,6 +213,7 @@ int alloc_batch_buffers(fvs_batch* B) {
 void init_view_constants(fvs_batch* B, DevView& d) {
   const fvs_options& ob = B->base;
   d.gamma = ob.gamma; d.gm1 = ob.gamma - 1.0; d.igm1 = 1.0 / (ob.gamma - 1.0);
+  d.ggm1 = ob.gamma / (ob.gamma - 1.0);
   d.khalf = ob.umuscl / 2.0; d.nkhalf = -ob.umuscl / 2.0; d.omk = 1.0 - ob.umuscl; d.cfl = ob.cfl;
   set_fp32_constants(d);
   d.limiter = ob.limiter; d.grad_method = ob.grad_method; d.first_order = ob.reconst == FVS_RECON_UPWIND1;

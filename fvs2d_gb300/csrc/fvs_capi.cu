@@ -16,6 +16,7 @@
 #include <vector>
 
 #include "df64.cuh"
+#include "fp64_fast.cuh"
 #include "fvs_internal.hpp"
 #include "fvs_layout.hpp"
 
@@ -96,6 +97,19 @@ __global__ void k_wall_loads(DevView d, int g0, int n, double c2, double p_inf, 
   }
   sums[0] = cn; sums[1] = ca; sums[2] = cn1; sums[3] = ca1;
   sums[4] = un_max; sums[5] = un_l2; sums[6] = un_l1;
+}
+
+// out[5i..5i+4] = rcp_nr(x), 1/x, rsqrt_nr(x), sqrt_nr(x), sqrt(x)
+__global__ void k_check_fp64_math(const double* __restrict__ x, int n, double* __restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double v = x[i];
+  double* o = out + 5 * (size_t)i;
+  o[0] = rcp_nr(v);
+  o[1] = 1.0 / v;
+  o[2] = rsqrt_nr(v);
+  o[3] = sqrt_nr(v);
+  o[4] = sqrt(v);
 }
 
 }  // namespace
@@ -382,6 +396,7 @@ int fvs_create(const fvs_mesh* mesh, const fvs_options* opt, fvs_handle** out) {
   d.cfl = H->o.cfl;
   d.gm1 = H->o.gamma - 1.0;
   d.igm1 = 1.0 / (H->o.gamma - 1.0);
+  d.ggm1 = H->o.gamma / (H->o.gamma - 1.0);
   set_fp32_constants(d);
   d.limiter = H->o.limiter;
   d.grad_method = H->o.grad_method;
@@ -765,6 +780,21 @@ int fvs_launches_per_step(const fvs_handle* h, int32_t* n) {
   if (!h || !n) return FVS_ERR_INVALID;
   *n = h->launches_per_step;
   return FVS_OK;
+}
+
+int fvs_check_fp64_math(const double* x, int32_t n, double* out) {
+  if (!x || !out || n <= 0) return FVS_ERR_INVALID;
+  double* d = nullptr;
+  const size_t nb = sizeof(double) * (size_t)n;
+  if (cudaMalloc(&d, 6 * nb) != cudaSuccess) return FVS_ERR_NOMEM;
+  cudaError_t e = cudaMemcpy(d, x, nb, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) {
+    k_check_fp64_math<<<(n + 255) / 256, 256>>>(d, n, d + n);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpy(out, d + n, 5 * nb, cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  return e == cudaSuccess ? FVS_OK : FVS_ERR_CUDA;
 }
 
 int fvs_device_state(fvs_handle* h, void** dptr) {

@@ -133,7 +133,7 @@ struct DevView {
   double* tctl = nullptr;         // [0] = t1, [1] = told of the current step
   // scheme
   double gamma = 1.4, khalf = 0, nkhalf = 0, omk = 1, cfl = 1, dt = 0;
-  double gm1 = 0.4, igm1 = 2.5;  // gamma-1 and 1/(gamma-1)
+  double gm1 = 0.4, igm1 = 2.5, ggm1 = 3.5;  // gamma-1, 1/(gamma-1) and gamma/(gamma-1)
   // the same constants rounded once on the host for the FP32 kernels
   float fgamma = 1.4f, fgm1 = 0.4f, figm1 = 2.5f, fkhalf = 0, fnkhalf = 0, fomk = 1;
   // and split into FP32 pairs (hi, lo) for the double-float kernels

