@@ -21,8 +21,9 @@
 // partial matrix C + z * split_stride (raw accumulators, no epilogue);
 // k_sum_splits adds the partials in order (deterministic).
 // Every mbarrier wait is bounded (clock64 budget).  On expiry the kernel sets
-// *err, waits (bounded) for the MMAs it issued, frees its tensor memory and
-// returns.
+// *err, skips the remaining K blocks and the epilogue, waits for the MMAs it
+// already issued (bounded, up to 9 budgets in all), frees its tensor memory
+// and returns.
 #pragma once
 
 #include <cuda_bf16.h>
@@ -206,9 +207,23 @@ __global__ void __launch_bounds__(THREADS) k_gemm_tc(const bf16* __restrict__ A,
       issued = kb;
     }
   }
-  // all MMAs issued: the last commit completes after every earlier MMA
+  // Every MMA this CTA issued must be complete before its tensor memory is
+  // read or freed, and before the CTA exits (the MMAs read the operand
+  // stages in shared memory).  The commit of the last issued block tracks
+  // all earlier MMAs of thread 0, so one wait on it covers them all; this
+  // wait also runs after an earlier wait ran out (s_ok == 0, loop left
+  // early).  The MMAs' operands are staged and nothing else gates them, so
+  // the tensor core completes them; only a GPU stalled for the whole budget
+  // makes the wait expire.  Then it is repeated once with 8 times the
+  // budget, and the CTA frees its tensor memory only after that: freeing it
+  // earlier could let a later CTA's accumulator receive these MMAs' writes.
   if (tid == 0 && issued >= 0) {
-    if (!mbar_wait(smem_u32(&mbar[issued & 1]), (uint32_t)((issued >> 1) & 1))) s_ok = 0;
+    const uint32_t fb = smem_u32(&mbar[issued & 1]), fp = (uint32_t)((issued >> 1) & 1);
+    if (!mbar_wait(fb, fp)) {
+      s_ok = 0;
+      for (int r = 0; r < 8 && !mbar_wait(fb, fp); r++) {
+      }
+    }
   }
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
