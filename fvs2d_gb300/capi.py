@@ -88,6 +88,7 @@ SIGNATURES = {
     "fvs_launches_per_step": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32)]),
     "fvs_device_state": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
     "fvs_check_fp64_math": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p]),
+    "fvs_tile_plan_info": (C.c_int, [C.POINTER(FvsMesh), C.POINTER(FvsOptions), C.c_void_p]),
     "fvs_batch_create": (C.c_int, [C.POINTER(FvsMesh), C.POINTER(FvsOptions), C.c_int32, C.c_int32, C.POINTER(C.c_void_p)]),
     "fvs_batch_destroy": (None, [C.c_void_p]),
     "fvs_batch_last_error": (C.c_char_p, [C.c_void_p]),

@@ -8,6 +8,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <deque>
 #include <memory>
@@ -19,6 +20,7 @@
 #include "fp64_fast.cuh"
 #include "fvs_internal.hpp"
 #include "fvs_layout.hpp"
+#include "fvs_tiles.hpp"
 
 using namespace fvs;
 
@@ -140,6 +142,16 @@ struct fvs_handle {
   bool host_only = false;
   double* d_wall = nullptr;  // wall-load scratch, allocated on first use
   size_t wall_cap = 0;
+  // fused RK stage (mixed and double-float): cells in tile order, one
+  // launch per stage (k_tile_stage)
+  bool fused = false;
+  TileView tv;
+  // d with one norm partial per tile block, for the fused stage
+  DevView tile_view() const {
+    DevView v = d;
+    v.nblk_red = tv.ntiles;
+    return v;
+  }
 
   ~fvs_handle() {
     if (d_wall) cudaFree(d_wall);
@@ -163,13 +175,70 @@ struct fvs_handle {
 
 namespace {
 
+// The fused RK stage runs for mixed and double-float handles unless the
+// environment variable FVS2D_TILE_STAGE is "0" at fvs_create.
+bool want_fused(const fvs_handle* H) {
+  if (H->o.precision != FVS_PREC_MIXED && H->o.precision != FVS_PREC_FP64_DF) return false;
+  const char* e = std::getenv("FVS2D_TILE_STAGE");
+  return !(e && e[0] == '0' && e[1] == 0);
+}
+
+// Tile plan of a fused handle from its device-order layout: plan arrays,
+// the extra primitive buffers (two in all for an even number of stages,
+// three for an odd one, so that every step starts and ends in Pv) and the
+// tile block's shared memory.  Returns false (handle stays unfused) when a
+// tile block would need more shared memory than a block may have.
+template <typename T>
+int build_tiles(fvs_handle* H, const Layout<T>& L, const std::vector<int>& tile_start, bool& ok) {
+  ok = false;
+  TilePlan P;
+  std::string err;
+  int rc = build_tile_plan(tile_start, L.ecell, L.cf, L.st_ptr, L.st_cell, P, err);
+  if (rc) return H->fail(rc, err);
+  err = check_tile_plan(P, L.nc, L.ne, L.ecell, L.cf, L.st_ptr);
+  if (!err.empty()) return H->fail(FVS_ERR_MESH, "tile plan: " + err);
+  TileView& tv = H->tv;
+  tv.ntiles = P.ntiles;
+  tv.lmax = P.lmax;
+  tv.gmax = P.gmax;
+  tv.fmax = P.fmax;
+  tv.smem_bytes = H->ks->tile_smem(P.lmax, P.gmax, P.fmax);
+  if (tv.smem_bytes == 0) return FVS_OK;
+  int *c0, *h0, *nh1, *halo, *g0, *lsp, *s0, *f0, *face;
+  uint16_t* lst;
+  uint32_t* flr;
+  int2* lcf;
+  DeviceArena& A = H->arena;
+  bool up = A.upload(c0, P.c0) && A.upload(h0, P.h0) && A.upload(nh1, P.nh1) && A.upload(halo, P.halo) &&
+            A.upload(g0, P.g0) && A.upload(lsp, P.lsp) && A.upload(s0, P.s0) && A.upload(lst, P.lst) &&
+            A.upload(f0, P.f0) && A.upload(face, P.face) && A.upload(flr, P.flr) && A.upload(lcf, P.lcf);
+  tv.c0 = c0; tv.h0 = h0; tv.nh1 = nh1; tv.halo = halo; tv.g0 = g0; tv.lsp = lsp; tv.s0 = s0; tv.lst = lst;
+  tv.f0 = f0; tv.face = face; tv.flr = flr; tv.lcf = lcf;
+  tv.nbuf = H->o.rk_nstages % 2 == 0 ? 2 : 3;
+  tv.Pbuf[0] = H->d.Pv;
+  for (int k = 1; k < tv.nbuf && up; k++) up = A.alloc(tv.Pbuf[k], sizeof(T) * 4 * (size_t)L.nc);
+  if (!up) return H->fail(FVS_ERR_NOMEM, "device allocation or upload of the tile plan failed");
+  ok = true;
+  return FVS_OK;
+}
+
 // Builds every device array of the handle from the host mesh.
 template <typename T>
 int build_device(fvs_handle* H) {
   Layout<T> L;
   std::string err;
   const bool fold_w = H->o.precision != FVS_PREC_FP64_STRICT;
-  int rc = append_case(L, H->hm, fold_w, 0, err);
+  const bool fuse = want_fused(H);
+  std::vector<int> tile_start;
+  int rc;
+  if (fuse) {
+    // tiles of compact patches (recursive coordinate bisection), reverse
+    // Cuthill-McKee order within each tile
+    const std::vector<int> order = rcb_tile_order(H->hm, rcm_order(H->hm), TILE_CELLS, tile_start);
+    rc = append_case(L, H->hm, fold_w, 0, err, &order);
+  } else {
+    rc = append_case(L, H->hm, fold_w, 0, err);
+  }
   if (rc) return H->fail(rc, err);
   H->perm = L.perm;
   DevView& d = H->d;
@@ -186,6 +255,10 @@ int build_device(fvs_handle* H) {
   std::vector<T> phi0(L.nc, T(H->o.reconst == FVS_RECON_UPWIND1 ? 0.0 : 1.0));
   if (cudaMemcpy(d.phi, phi0.data(), sizeof(T) * L.nc, cudaMemcpyHostToDevice) != cudaSuccess)
     return H->fail(FVS_ERR_CUDA, "phi upload failed");
+  if (fuse && H->ks->tile_stage) {
+    rc = build_tiles<T>(H, L, tile_start, H->fused);
+    if (rc) return rc;
+  }
   return FVS_OK;
 }
 
@@ -216,6 +289,11 @@ void enqueue_step(fvs_handle* H) {
   const KernelSet& K = *H->ks;
   cudaStream_t s = H->stream;
   K.begin_step(H->d, s);
+  if (H->fused) {
+    const DevView dv = H->tile_view();
+    for (size_t k = 0; k < H->stages.size(); k++) K.tile_stage(dv, H->tv, H->stages[k], (int)k, s);
+    return;
+  }
   for (const StageParams& sp : H->stages) {
     K.gradient(H->d, s);
     K.flux(H->d, sp.dts, s);
@@ -224,9 +302,9 @@ void enqueue_step(fvs_handle* H) {
 }
 
 int count_launches(const fvs_handle* H) {
-  // k_begin_step, then gradient (second order), flux and update per stage;
-  // the last update also reduces the norms
-  int per_stage = (H->d.first_order ? 0 : 1) + 2;
+  // k_begin_step, then gradient (second order), flux and update per stage,
+  // or one fused tile stage; the last stage also reduces the norms
+  int per_stage = H->fused ? 1 : (H->d.first_order ? 0 : 1) + 2;
   return 1 + per_stage * (int)H->stages.size();
 }
 
@@ -756,13 +834,21 @@ int fvs_profile_step(fvs_handle* h, int32_t cap, int32_t* n, char* names, float*
   };
   mark("start");
   K.begin_step(h->d, s);
-  for (const StageParams& sp : h->stages) {
-    K.gradient(h->d, s);
-    mark("gradient");
-    K.flux(h->d, sp.dts, s);
-    mark("flux");
-    K.update(h->d, sp, s);
-    mark("update");
+  if (h->fused) {
+    const DevView dv = h->tile_view();
+    for (size_t k = 0; k < h->stages.size(); k++) {
+      K.tile_stage(dv, h->tv, h->stages[k], (int)k, s);
+      mark("tile_stage");
+    }
+  } else {
+    for (const StageParams& sp : h->stages) {
+      K.gradient(h->d, s);
+      mark("gradient");
+      K.flux(h->d, sp.dts, s);
+      mark("flux");
+      K.update(h->d, sp, s);
+      mark("update");
+    }
   }
   cudaError_t e = cudaStreamSynchronize(s);
   if (e != cudaSuccess) return h->cuda_fail(e, "profile step");
@@ -779,6 +865,31 @@ int fvs_profile_step(fvs_handle* h, int32_t cap, int32_t* n, char* names, float*
 int fvs_launches_per_step(const fvs_handle* h, int32_t* n) {
   if (!h || !n) return FVS_ERR_INVALID;
   *n = h->launches_per_step;
+  return FVS_OK;
+}
+
+int fvs_tile_plan_info(const fvs_mesh* mesh, const fvs_options* opt, int32_t* info) {
+  if (!mesh || !opt || !info) return FVS_ERR_INVALID;
+  std::string err;
+  int rc = validate_options(opt, err);
+  if (rc) { g_create_error = err; return rc; }
+  fvs_options o = *opt;
+  if (o.reconst != FVS_RECON_UMUSCL) o.umuscl = 0.0;
+  HostMesh hm;
+  rc = build_host_mesh(mesh, &o, hm, err);
+  if (rc) { g_create_error = err; return rc; }
+  std::vector<int> tile_start;
+  const std::vector<int> order = rcb_tile_order(hm, rcm_order(hm), TILE_CELLS, tile_start);
+  Layout<float> L;
+  rc = append_case(L, hm, true, 0, err, &order);
+  if (rc) { g_create_error = err; return rc; }
+  TilePlan P;
+  rc = build_tile_plan(tile_start, L.ecell, L.cf, L.st_ptr, L.st_cell, P, err);
+  if (rc) { g_create_error = err; return rc; }
+  const std::string bad = check_tile_plan(P, L.nc, L.ne, L.ecell, L.cf, L.st_ptr);
+  info[0] = P.ntiles; info[1] = P.lmax; info[2] = P.gmax; info[3] = P.fmax; info[4] = bad.empty() ? 1 : 0;
+  info[5] = (int32_t)P.halo.size();
+  if (!bad.empty()) { g_create_error = bad; return FVS_ERR_MESH; }
   return FVS_OK;
 }
 

@@ -158,6 +158,30 @@ inline void set_fp32_constants(DevView& d) {
   split(d.khalf, d.dkhalf); split(d.nkhalf, d.dnkhalf); split(d.omk, d.domk);
 }
 
+// Device view of a TilePlan (fvs_tiles.hpp) for the fused RK stage: one
+// thread block per tile keeps the primitives of the tile and its halo, the
+// gradients of the tile and its first halo layer and the tile's face fluxes
+// in shared memory.  Arrays as in TilePlan; Pbuf: the primitive buffers the
+// stages alternate between (Pbuf[0] is DevView::Pv).
+struct TileView {
+  int ntiles = 0, lmax = 0, gmax = 0, fmax = 0;
+  const int* c0 = nullptr;
+  const int* h0 = nullptr;
+  const int* nh1 = nullptr;
+  const int* halo = nullptr;
+  const int* g0 = nullptr;
+  const int* lsp = nullptr;
+  const int* s0 = nullptr;
+  const uint16_t* lst = nullptr;
+  const int* f0 = nullptr;
+  const int* face = nullptr;
+  const uint32_t* flr = nullptr;
+  const int2* lcf = nullptr;
+  void* Pbuf[3] = {nullptr, nullptr, nullptr};
+  int nbuf = 2;
+  size_t smem_bytes = 0;  // dynamic shared memory of one block
+};
+
 struct StageParams {
   int stage = 1, nstages = 4, mode = MODE_RK, steady = 0, last = 0;
   double h = 0;       // h_rk(stage) (unsteady)
@@ -217,6 +241,12 @@ struct KernelSet {
   cudaError_t (*persistent)(const DevView&, const PersistPlan&, int grid, int block, cudaStream_t);
   // one step of the same tile work as separate launches (for graph capture)
   cudaError_t (*tiled_step)(const DevView&, const PersistPlan&, int block, cudaStream_t);
+  // fused RK stage over the tiles of a TileView (mixed and double-float
+  // builds; null elsewhere): stage k (0-based) reads Pbuf[k % nbuf] and
+  // writes Pbuf[(k + 1) % nbuf]; dts is the stage's time offset
+  cudaError_t (*tile_stage)(const DevView&, const TileView&, const StageParams&, int k, cudaStream_t);
+  // shared memory of one tile block for the plan's largest tile (bytes)
+  size_t (*tile_smem)(int lmax, int gmax, int fmax);
 };
 // Defect correction of a first-order steady batch (mixed build): per chunk
 // the FP64 residual R0 of the base state is evaluated once; the RK stages

@@ -10,7 +10,8 @@ namespace fvs {
 const KernelSet& kernels_mixed() {
   static const KernelSet k = {"mixed", k_mixed::launch_begin_step, k_mixed::launch_cvar2pvar, k_mixed::launch_gradient,
                               k_mixed::launch_flux, k_mixed::launch_update, k_mixed::launch_residual_out, k_mixed::persistent_occupancy,
-                              k_mixed::launch_persistent, k_mixed::launch_tiled_step};
+                              k_mixed::launch_persistent, k_mixed::launch_tiled_step,
+                              k_mixed::launch_tile_stage, k_mixed::tile_smem};
   return k;
 }
 const DcKernels& dc_kernels() {

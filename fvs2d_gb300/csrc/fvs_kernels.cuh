@@ -348,11 +348,14 @@ __device__ __forceinline__ void roe_flux_area_fp64(double gm1, double ggm1, cons
 // ---------------------------------------------------------------------------
 // gradient (+ limiter) : one thread per cell
 // ---------------------------------------------------------------------------
-template <int METHOD, int LIM, bool COH>
-__device__ __forceinline__ void gradient_item(const DevView& d, int ic) {
-  const T* P = static_cast<const T*>(d.Pv);
-  T pc[4], gx[4], gy[4], pmin[4], pmax[4];
-  ldc4<COH>(P, ic, pc);
+// Gradient (and limiter) of cell ic from its primitives pc; load(k, pj)
+// fills pj with the primitives of stencil entry k (global CSR index).
+// Shared by the separate gradient kernel (loads from global memory) and the
+// fused tile stage (loads from shared memory): the same arithmetic.
+template <int METHOD, int LIM, class Load>
+__device__ __forceinline__ void gradient_core(const DevView& d, int ic, const T* pc, Load load, T* gx, T* gy,
+                                              T& phi_out) {
+  T pmin[4], pmax[4];
 #pragma unroll
   for (int v = 0; v < 4; v++) { pmin[v] = pc[v]; pmax[v] = pc[v]; }
   const int b = d.st_ptr[ic], e = d.st_ptr[ic + 1];
@@ -365,9 +368,8 @@ __device__ __forceinline__ void gradient_item(const DevView& d, int ic) {
     const T* __restrict__ W = static_cast<const T*>(d.st_w);
 #endif
     for (int k = b; k < e; k++) {
-      const int jc = d.st_cell[k];
       T pj[4];
-      ldc4<COH>(P, jc, pj);
+      load(k, pj);
       const T2 c = ld2(d.st_coef, k);
 #if FVS_STRICT
       const T w = W[k];
@@ -396,7 +398,7 @@ __device__ __forceinline__ void gradient_item(const DevView& d, int ic) {
     for (int v = 0; v < 4; v++) { gx[v] = c0.x * pc[v]; gy[v] = c0.y * pc[v]; }
     for (int k = b; k < e; k++) {
       T pj[4];
-      ldc4<COH>(P, d.st_cell[k], pj);
+      load(k, pj);
       const T2 c = ld2(d.st_coef, k);
 #pragma unroll
       for (int v = 0; v < 4; v++) { gx[v] = gx[v] + c.x * pj[v]; gy[v] = gy[v] + c.y * pj[v]; }
@@ -418,7 +420,7 @@ __device__ __forceinline__ void gradient_item(const DevView& d, int ic) {
     const T* __restrict__ CN = static_cast<const T*>(d.st_coef);
     for (int k = b; k < e; k++) {
       T pj[4];
-      ldc4<COH>(P, d.st_cell[k], pj);
+      load(k, pj);
       const T cn = CN[k];
       const T2 ce = ld2(d.coefedg, 4 * ic + d.st_node[k]);
 #pragma unroll
@@ -434,8 +436,6 @@ __device__ __forceinline__ void gradient_item(const DevView& d, int ic) {
     for (int v = 0; v < 4; v++) { gx[v] = gx[v] * rv; gy[v] = gy[v] * rv; }
 #endif
   }
-  st4(static_cast<T*>(d.Gx), ic, gx);
-  st4(static_cast<T*>(d.Gy), ic, gy);
   if (LIM) {
     // compute_gradient_limiter, src/gradient_limiter.f90:47-88
     const int nv = d.nvrt[ic];
@@ -462,8 +462,19 @@ __device__ __forceinline__ void gradient_item(const DevView& d, int ic) {
       const T ph = mv < T(1) ? mv : T(1);
       phimin = (v == 0 || ph < phimin) ? ph : phimin;
     }
-    static_cast<T*>(d.phi)[ic] = phimin;
+    phi_out = phimin;
   }
+}
+
+template <int METHOD, int LIM, bool COH>
+__device__ __forceinline__ void gradient_item(const DevView& d, int ic) {
+  const T* P = static_cast<const T*>(d.Pv);
+  T pc[4], gx[4], gy[4], ph;
+  ldc4<COH>(P, ic, pc);
+  gradient_core<METHOD, LIM>(d, ic, pc, [&](int k, T* pj) { ldc4<COH>(P, d.st_cell[k], pj); }, gx, gy, ph);
+  st4(static_cast<T*>(d.Gx), ic, gx);
+  st4(static_cast<T*>(d.Gy), ic, gy);
+  if (LIM) static_cast<T*>(d.phi)[ic] = ph;
 }
 
 template <int METHOD, int LIM>
@@ -545,15 +556,13 @@ __device__ __forceinline__ void ghost_state(const DevView& d, int rec, double ti
 // values) and no gradient is read.
 enum : int { REC_GENERAL = 0, REC_SPEC = 1, REC_FIRST = 2 };
 
-// Roe flux of one edge slot from its face states, times the face length,
-// into the slot's record; the wave speed times the length likewise
-__device__ __forceinline__ void flux_finish(const DevView& d, int e, const T* pfL, const T* pfR, T2 n, T af) {
-  T flux[4], wsm;
+// Roe flux of one edge slot from its face states, times the face length
+// (flux) and the wave speed times the length (wsa)
+__device__ __forceinline__ void flux_eval(const DevView& d, const T* pfL, const T* pfR, T2 n, T af, T* flux, T& wsa) {
 #if FVS_FP64_FAST
-  roe_flux_area_fp64(d.gm1, d.ggm1, pfL, pfR, n.x, n.y, af, flux, wsm);
-  st4(static_cast<T*>(d.eflux), e, flux);
-  static_cast<T*>(d.ews)[e] = wsm;
+  roe_flux_area_fp64(d.gm1, d.ggm1, pfL, pfR, n.x, n.y, af, flux, wsa);
 #else
+  T wsm;
 #if FVS_STRICT
   roe_flux(T(d.gamma), pfL, pfR, n.x, n.y, flux, wsm);
 #else
@@ -561,43 +570,43 @@ __device__ __forceinline__ void flux_finish(const DevView& d, int e, const T* pf
 #endif
 #pragma unroll
   for (int v = 0; v < 4; v++) flux[v] = flux[v] * af;
-  st4(static_cast<T*>(d.eflux), e, flux);
-  static_cast<T*>(d.ews)[e] = wsm * af;
+  wsa = wsm * af;
 #endif
 }
 
-template <int REC, bool COH>
-__device__ __forceinline__ void flux_item(const DevView& d, int e, double time) {
+// ... into the slot's record
+__device__ __forceinline__ void flux_finish(const DevView& d, int e, const T* pfL, const T* pfR, T2 n, T af) {
+  T flux[4], wsa;
+  flux_eval(d, pfL, pfR, n, af, flux, wsa);
+  st4(static_cast<T*>(d.eflux), e, flux);
+  static_cast<T*>(d.ews)[e] = wsa;
+}
+
+// Face states of edge slot e (src/residual.f90:83-92 interior, :128-137
+// boundary) from the data of its L cell (pl, gxl, gyl, phiL) and, on an
+// interior slot, its R cell; a boundary slot's right state is the ghost
+// state.  REC_FIRST reads no gradient; REC_SPEC no limiter value.  Shared by
+// the edge-flux kernel and the fused tile stage: the same arithmetic.
+template <int REC>
+__device__ __forceinline__ void face_states(const DevView& d, int e, bool interior, double time, T2 n, const T* pl,
+                                            const T* gxl, const T* gyl, T phiL, const T* pr, const T* gxr,
+                                            const T* gyr, T phiR, T* pfL, T* pfR) {
   constexpr bool SPEC = REC == REC_SPEC;
-  const T* P = static_cast<const T*>(d.Pv);
-  const T* GX = static_cast<const T*>(d.Gx);
-  const T* GY = static_cast<const T*>(d.Gy);
-  const T* PH = static_cast<const T*>(d.phi);
-  const int2 lr = d.ecell[e];
-  const T2 n = ld2(d.enrm, e);
-  const T af = static_cast<const T*>(d.earea)[e];
-  T pl[4], gxl[4], gyl[4], pfL[4], pfR[4];
-  ldc4<COH>(P, lr.x, pl);
   if (REC == REC_FIRST) {
 #pragma unroll
     for (int v = 0; v < 4; v++) pfL[v] = pl[v];
-    if (lr.y >= 0) {
-      ldc4<COH>(P, lr.y, pfR);
+    if (interior) {
+#pragma unroll
+      for (int v = 0; v < 4; v++) pfR[v] = pr[v];
     } else {
       const T2 xy = ld2(d.exy, e);
       ghost_state(d, d.ebtype[e], time, xy.x, xy.y, n.x, n.y, pfL, pfR);
     }
-  } else {
+    return;
+  }
   const T2 dl = ld2(d.edL, e);
-  ldc4<COH>(GX, lr.x, gxl);
-  ldc4<COH>(GY, lr.x, gyl);
-  const T phiL = SPEC ? T(1) : ldc1<COH>(PH, lr.x);
-  if (lr.y >= 0) {
+  if (interior) {
     // src/residual.f90:83-92
-    T pr[4], gxr[4], gyr[4];
-    ldc4<COH>(P, lr.y, pr);
-    ldc4<COH>(GX, lr.y, gxr);
-    ldc4<COH>(GY, lr.y, gyr);
     const T2 dr = ld2(d.edR, e);
     if (SPEC) {
 #pragma unroll
@@ -612,7 +621,6 @@ __device__ __forceinline__ void flux_item(const DevView& d, int e, double time) 
 #endif
       }
     } else {
-      const T phiR = ldc1<COH>(PH, lr.y);
       const T kh = TP(khalf), nkh = TP(nkhalf), omk = TP(omk);
 #pragma unroll
       for (int v = 0; v < 4; v++) {
@@ -631,7 +639,36 @@ __device__ __forceinline__ void flux_item(const DevView& d, int e, double time) 
     const T2 xy = ld2(d.exy, e);
     ghost_state(d, d.ebtype[e], time, xy.x, xy.y, n.x, n.y, pfL, pfR);
   }
+}
+
+template <int REC, bool COH>
+__device__ __forceinline__ void flux_item(const DevView& d, int e, double time) {
+  constexpr bool SPEC = REC == REC_SPEC;
+  const T* P = static_cast<const T*>(d.Pv);
+  const T* GX = static_cast<const T*>(d.Gx);
+  const T* GY = static_cast<const T*>(d.Gy);
+  const T* PH = static_cast<const T*>(d.phi);
+  const int2 lr = d.ecell[e];
+  const T2 n = ld2(d.enrm, e);
+  const T af = static_cast<const T*>(d.earea)[e];
+  const bool interior = lr.y >= 0;
+  T pl[4], gxl[4], gyl[4], pr[4], gxr[4], gyr[4], pfL[4], pfR[4];
+  T phiL = T(1), phiR = T(1);
+  ldc4<COH>(P, lr.x, pl);
+  if (REC != REC_FIRST) {
+    ldc4<COH>(GX, lr.x, gxl);
+    ldc4<COH>(GY, lr.x, gyl);
+    if (!SPEC) phiL = ldc1<COH>(PH, lr.x);
   }
+  if (interior) {
+    ldc4<COH>(P, lr.y, pr);
+    if (REC != REC_FIRST) {
+      ldc4<COH>(GX, lr.y, gxr);
+      ldc4<COH>(GY, lr.y, gyr);
+      if (!SPEC) phiR = ldc1<COH>(PH, lr.y);
+    }
+  }
+  face_states<REC>(d, e, interior, time, n, pl, gxl, gyl, phiL, pr, gxr, gyr, phiR, pfL, pfR);
   flux_finish(d, e, pfL, pfR, n, af);
 }
 
@@ -726,26 +763,36 @@ __device__ __forceinline__ double to_double(df64 x) { return f2d_bits(x.hi) + f2
 
 // df64 flux slots summed in df64 in the reference's order, times 1/vol in
 // df64, then one FP64 addition per component
-template <bool WS, bool COH>
-__device__ __forceinline__ void cell_residual(const DevView& d, int ic, double* res, double& ws) {
+// flux records of a cell's faces in its gather order (see
+// residual_from_faces_f), summed in df64, times -1/vol in df64
+template <bool WS, class Get>
+__device__ __forceinline__ void residual_from_faces_df(const int* sl, df64 rv, Get get, double* res, double& ws) {
   df64 r[4] = {df64(0.f, 0.f), df64(0.f, 0.f), df64(0.f, 0.f), df64(0.f, 0.f)}, w(0.f, 0.f);
-  const int4 cf = d.cflist[ic];
-  const int sl[4] = {cf.x, cf.y, cf.z, cf.w};
 #pragma unroll
   for (int j = 0; j < 4; j++) {
     const int s = sl[j];
     if (s == 0) continue;
     const int idx = (s > 0 ? s : -s) - 1;
-    df64 f[4];
-    ldc4<COH>(static_cast<const df64*>(d.eflux), idx, f);
+    df64 f[4], wf(0.f, 0.f);
+    get(idx, f, wf);
 #pragma unroll
     for (int v = 0; v < 4; v++) r[v] = s > 0 ? r[v] + f[v] : r[v] - f[v];
-    if (WS) w = w + ldc1<COH>(static_cast<const df64*>(d.ews), idx);
+    if (WS) w = w + wf;
   }
-  const df64 rv = -static_cast<const df64*>(d.volT)[ic];
 #pragma unroll
   for (int v = 0; v < 4; v++) res[v] = to_double(r[v] * rv);
   ws = WS ? to_double(w) : 0.0;
+}
+
+template <bool WS, bool COH>
+__device__ __forceinline__ void cell_residual(const DevView& d, int ic, double* res, double& ws) {
+  const int4 cf = d.cflist[ic];
+  const int sl[4] = {cf.x, cf.y, cf.z, cf.w};
+  const df64 rv = -static_cast<const df64*>(d.volT)[ic];
+  residual_from_faces_df<WS>(sl, rv, [&](int idx, df64* f, df64& w) {
+    ldc4<COH>(static_cast<const df64*>(d.eflux), idx, f);
+    if (WS) w = ldc1<COH>(static_cast<const df64*>(d.ews), idx);
+  }, res, ws);
 }
 #else
 template <bool WS, bool COH>
@@ -840,25 +887,38 @@ __device__ __forceinline__ void block_sum4(const double* v, double* out) {
 // of the increment, below the FP32 flux rounding already in R) and added to
 // the FP64 state: 4-8 FP64 additions per cell and stage instead of ~30 FP64
 // operations.  The accumulator F is stored as FP32 (float4 per cell).
-__device__ __forceinline__ void cell_residual_f(const DevView& d, int ic, bool want_ws, float* res, float& ws) {
+// The flux records of a cell's faces summed in its gather order: sl holds
+// four signed references (+-(record + 1), 0: none), get(idx, f, w) loads
+// record idx (w only when want_ws).  Shared by the update kernel (records in
+// global memory) and the fused tile stage (records in shared memory).
+template <class Get>
+__device__ __forceinline__ void residual_from_faces_f(const int* sl, float rv, bool want_ws, Get get, float* res,
+                                                      float& ws) {
   float hi[4] = {0.f, 0.f, 0.f, 0.f}, lo[4] = {0.f, 0.f, 0.f, 0.f}, wh = 0.f, wl = 0.f;
-  const int4 cf = d.cflist[ic];
-  const int sl[4] = {cf.x, cf.y, cf.z, cf.w};
 #pragma unroll
   for (int j = 0; j < 4; j++) {
     const int s = sl[j];
     if (s == 0) continue;
     const int idx = (s > 0 ? s : -s) - 1;
-    float f[4];
-    ldc4<true>(static_cast<const float*>(d.eflux), idx, f);
+    float f[4], w = 0.f;
+    get(idx, f, w);
 #pragma unroll
     for (int v = 0; v < 4; v++) two_sum(hi[v], lo[v], s > 0 ? f[v] : -f[v]);
-    if (want_ws) two_sum(wh, wl, ldc1<true>(static_cast<const float*>(d.ews), idx));
+    if (want_ws) two_sum(wh, wl, w);
   }
-  const float rv = -static_cast<const float*>(d.volT)[ic];
 #pragma unroll
   for (int v = 0; v < 4; v++) res[v] = (hi[v] + lo[v]) * rv;
   ws = wh + wl;
+}
+
+__device__ __forceinline__ void cell_residual_f(const DevView& d, int ic, bool want_ws, float* res, float& ws) {
+  const int4 cf = d.cflist[ic];
+  const int sl[4] = {cf.x, cf.y, cf.z, cf.w};
+  const float rv = -static_cast<const float*>(d.volT)[ic];
+  residual_from_faces_f(sl, rv, want_ws, [&](int idx, float* f, float& w) {
+    ldc4<true>(static_cast<const float*>(d.eflux), idx, f);
+    if (want_ws) w = ldc1<true>(static_cast<const float*>(d.ews), idx);
+  }, res, ws);
 }
 
 // the RK stage of one cell from its residual res (and, at a steady first
@@ -945,13 +1005,13 @@ __device__ __forceinline__ void update_item(const DevView& d, const StageParams&
 }
 
 #else
-// one cell of an RK stage; at the last stage adds |U-U0|^2 to d2
+// the RK stage of one cell from its residual res (and, at a steady first
+// stage, its wave-speed sum ws); the new primitives go to Pout; at the last
+// stage adds |U-U0|^2 to d2
 template <int MODE, bool COH>
-__device__ __forceinline__ void update_item(const DevView& d, const StageParams& sp, int ic, double* d2) {
+__device__ __forceinline__ void apply_stage_d(const DevView& d, const StageParams& sp, int ic, const double* res,
+                                              double ws, T* Pout, double* d2) {
   {
-    double res[4], ws;
-    if (sp.steady && sp.stage == 1) cell_residual<true, COH>(d, ic, res, ws);
-    else cell_residual<false, COH>(d, ic, res, ws);
     double h = sp.h;
     if (sp.steady) {
       double dtl;
@@ -1007,7 +1067,7 @@ __device__ __forceinline__ void update_item(const DevView& d, const StageParams&
     st4(d.U, ic, u);
     T p[4];
     cons2prim(TP(gm1), u, p);
-    st4(static_cast<T*>(d.Pv), ic, p);
+    st4(Pout, ic, p);
     if (sp.last) {
 #pragma unroll
       for (int v = 0; v < 4; v++) {
@@ -1016,6 +1076,15 @@ __device__ __forceinline__ void update_item(const DevView& d, const StageParams&
       }
     }
   }
+}
+
+// one cell of an RK stage; at the last stage adds |U-U0|^2 to d2
+template <int MODE, bool COH>
+__device__ __forceinline__ void update_item(const DevView& d, const StageParams& sp, int ic, double* d2) {
+  double res[4], ws;
+  if (sp.steady && sp.stage == 1) cell_residual<true, COH>(d, ic, res, ws);
+  else cell_residual<false, COH>(d, ic, res, ws);
+  apply_stage_d<MODE, COH>(d, sp, ic, res, ws, static_cast<T*>(d.Pv), d2);
 }
 
 #endif  // FVS_MIXED
@@ -1041,29 +1110,201 @@ __device__ __forceinline__ void norm_final_block(const DevView& d) {
 // One RK stage over all cells.  At the last stage every block writes its
 // partial norms; the block that finishes last (a counter in stepctl[1])
 // reduces them, so no separate norm launch is needed.
+// the block's sum of d2 into partials[blockIdx.x]; the block that finishes
+// last (d.nblk_red == gridDim.x) reduces all partials into the step's norms
+__device__ __forceinline__ void stage_norms(const DevView& d, const double* d2) {
+  __shared__ int s_last;
+  double out[4];
+  block_sum4(d2, out);
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < 4; k++) d.partials[4 * blockIdx.x + k] = out[k];
+    __threadfence();
+    s_last = atomicAdd(&d.stepctl[1], 1) == (int)gridDim.x - 1;
+  }
+  __syncthreads();
+  if (s_last) {
+    __threadfence();
+    norm_final_block(d);
+    if (threadIdx.x == 0) d.stepctl[1] = 0;
+  }
+}
+
 template <int MODE>
 __global__ void __launch_bounds__(256) k_update(const DevView d, const StageParams sp) {
   const int ic = blockIdx.x * blockDim.x + threadIdx.x;
   double d2[4] = {0.0, 0.0, 0.0, 0.0};
   if (ic < d.nc) update_item<MODE, false>(d, sp, ic, d2);
-  if (sp.last) {
-    __shared__ int s_last;
-    double out[4];
-    block_sum4(d2, out);
-    if (threadIdx.x == 0) {
+  if (sp.last) stage_norms(d, d2);
+}
+
+#if FVS_MIXED || FVS_DF
+// ---------------------------------------------------------------------------
+// fused RK stage: one block per tile (fvs_tiles.hpp)
+// ---------------------------------------------------------------------------
+// Shared memory of a tile block: primitives of the tile, halo1 and halo2
+// (lmax x 4), gradients and limiter values of the tile and halo1 (gmax x 9),
+// and the flux * area and ws * area of the tile's faces (fmax x 5).
+static size_t tile_smem_bytes(int lmax, int gmax, int fmax) {
+  return sizeof(T) * (4 * (size_t)lmax + 9 * (size_t)gmax + 5 * (size_t)fmax);
+}
+
+// One RK stage of one tile in four phases separated by block barriers:
+//  1. primitives of the tile and its halos from global memory (buffer kin)
+//  2. gradient (and limiter) of every tile and halo1 cell from shared memory
+//     (gradient_core, the separate gradient kernel's arithmetic)
+//  3. face states and Roe flux of every face of the tile (face_states,
+//     flux_eval: the edge-flux kernel's arithmetic)
+//  4. per tile cell the face fluxes summed in the cell's gather order
+//     (the update kernel's order and arithmetic), the RK update of the
+//     conservative state, the new primitives into buffer kout and, at the
+//     last stage, the norm partials
+// Gradients and face fluxes never leave the chip.  A cut face (cells in two
+// tiles) is evaluated by both tiles with the same operands and the same
+// instructions, so both cells receive the same flux.  Results are
+// bit-identical to the separate gradient, flux and update kernels.
+template <int MODE, int REC, int LIM>
+__global__ void __launch_bounds__(256) k_tile_stage(const DevView d, const TileView tv, const StageParams sp, int kin,
+                                                   int kout) {
+  extern __shared__ __align__(16) unsigned char tile_shm[];
+  const int t = blockIdx.x, tid = threadIdx.x, nthr = blockDim.x;
+  const int b = tv.c0[t], n = tv.c0[t + 1] - b;
+  const int hb = tv.h0[t], nl = n + (tv.h0[t + 1] - hb), ng = n + tv.nh1[t];
+  T* sP = reinterpret_cast<T*>(tile_shm);
+  T* sGx = sP + 4 * (size_t)tv.lmax;
+  T* sGy = sGx + 4 * (size_t)tv.gmax;
+  T* sPh = sGy + 4 * (size_t)tv.gmax;
+  T* sF = sPh + tv.gmax;
+  const T* Pin = static_cast<const T*>(tv.Pbuf[kin]);
+  T* Pout = static_cast<T*>(tv.Pbuf[kout]);
+  // 1. primitives
+  for (int i = tid; i < nl; i += nthr) ld4(Pin, i < n ? b + i : tv.halo[hb + i - n], sP + 4 * i);
+  __syncthreads();
+  // 2. gradients of the tile and halo1 cells
+  if (REC != REC_FIRST) {
+    const uint16_t* lst = tv.lst + tv.s0[t];
+    const int* lsp = tv.lsp + tv.g0[t];
+    for (int i = tid; i < ng; i += nthr) {
+      const int gid = i < n ? b + i : tv.halo[hb + i - n];
+      const uint16_t* L = lst + lsp[i];
+      const int kb = d.st_ptr[gid];
+      auto load = [&](int k, T* pj) {
+        const T* q = sP + 4 * (int)L[k - kb];
 #pragma unroll
-      for (int k = 0; k < 4; k++) d.partials[4 * blockIdx.x + k] = out[k];
-      __threadfence();
-      s_last = atomicAdd(&d.stepctl[1], 1) == (int)gridDim.x - 1;
+        for (int v = 0; v < 4; v++) pj[v] = q[v];
+      };
+      T gx[4], gy[4], ph = T(1);
+      if (d.grad_method == FVS_GRAD_LSQ) gradient_core<FVS_GRAD_LSQ, LIM>(d, gid, sP + 4 * i, load, gx, gy, ph);
+      else if (d.grad_method == FVS_GRAD_GGCB) gradient_core<FVS_GRAD_GGCB, 0>(d, gid, sP + 4 * i, load, gx, gy, ph);
+      else gradient_core<FVS_GRAD_GGNB, 0>(d, gid, sP + 4 * i, load, gx, gy, ph);
+#pragma unroll
+      for (int v = 0; v < 4; v++) {
+        sGx[4 * i + v] = gx[v];
+        sGy[4 * i + v] = gy[v];
+      }
+      if (REC == REC_GENERAL) sPh[i] = LIM ? ph : static_cast<const T*>(d.phi)[gid];
     }
     __syncthreads();
-    if (s_last) {
-      __threadfence();
-      norm_final_block(d);
-      if (threadIdx.x == 0) d.stepctl[1] = 0;
-    }
   }
+  // 3. face fluxes
+  const double time = d.tctl[1] + sp.dts;
+  const int fb = tv.f0[t], nf = tv.f0[t + 1] - fb;
+  for (int f = tid; f < nf; f += nthr) {
+    const int e = tv.face[fb + f];
+    const uint32_t lr = tv.flr[fb + f];
+    const int l = (int)(lr & 0xFFFFu), rr = (int)(lr >> 16);
+    const bool interior = rr != 0xFFFF;
+    const int r = interior ? rr : l;  // a boundary slot reads no right cell
+    const T2 nn = ld2(d.enrm, e);
+    const T af = static_cast<const T*>(d.earea)[e];
+    T pfL[4], pfR[4], flux[4], wsa;
+    const T phiL = REC == REC_GENERAL ? sPh[l] : T(1), phiR = REC == REC_GENERAL ? sPh[r] : T(1);
+    face_states<REC>(d, e, interior, time, nn, sP + 4 * l, sGx + 4 * l, sGy + 4 * l, phiL, sP + 4 * r, sGx + 4 * r,
+                     sGy + 4 * r, phiR, pfL, pfR);
+    flux_eval(d, pfL, pfR, nn, af, flux, wsa);
+#pragma unroll
+    for (int v = 0; v < 4; v++) sF[5 * f + v] = flux[v];
+    sF[5 * f + 4] = wsa;
+  }
+  __syncthreads();
+  // 4. gather and RK update of the tile's cells
+  double d2[4] = {0.0, 0.0, 0.0, 0.0};
+  const bool want_ws = sp.steady && sp.stage == 1;
+  for (int i = tid; i < n; i += nthr) {
+    const int gid = b + i;
+    const int2 q = tv.lcf[gid];
+    const int sl[4] = {(int)(int16_t)(q.x & 0xFFFF), (int)(int16_t)((unsigned)q.x >> 16),
+                       (int)(int16_t)(q.y & 0xFFFF), (int)(int16_t)((unsigned)q.y >> 16)};
+    auto get = [&](int idx, T* f, T& w) {
+#pragma unroll
+      for (int v = 0; v < 4; v++) f[v] = sF[5 * idx + v];
+      w = sF[5 * idx + 4];
+    };
+#if FVS_MIXED
+    float res[4], ws;
+    residual_from_faces_f(sl, -static_cast<const float*>(d.volT)[gid], want_ws, get, res, ws);
+    apply_stage_f<MODE, false>(d, sp, gid, res, ws, Pout, d2);
+#else
+    double res[4], ws;
+    const df64 rv = -static_cast<const df64*>(d.volT)[gid];
+    if (want_ws) residual_from_faces_df<true>(sl, rv, get, res, ws);
+    else residual_from_faces_df<false>(sl, rv, get, res, ws);
+    apply_stage_d<MODE, false>(d, sp, gid, res, ws, Pout, d2);
+#endif
+  }
+  if (sp.last) stage_norms(d, d2);
 }
+
+template <int MODE, int REC, int LIM>
+static cudaError_t launch_tile_t(const DevView& d, const TileView& tv, const StageParams& sp, int k, cudaStream_t s) {
+  k_tile_stage<MODE, REC, LIM><<<tv.ntiles, 256, tv.smem_bytes, s>>>(d, tv, sp, k % tv.nbuf, (k + 1) % tv.nbuf);
+  return cudaGetLastError();
+}
+
+template <int MODE>
+static cudaError_t launch_tile_mode(const DevView& d, const TileView& tv, const StageParams& sp, int k,
+                                    cudaStream_t s) {
+  const bool spec = d.khalf == 0.0 && d.omk == 1.0 && d.limiter == FVS_LIM_NONE;
+  if (d.first_order) return launch_tile_t<MODE, REC_FIRST, 0>(d, tv, sp, k, s);
+  if (spec) return launch_tile_t<MODE, REC_SPEC, 0>(d, tv, sp, k, s);
+  if (d.limiter != FVS_LIM_NONE) return launch_tile_t<MODE, REC_GENERAL, 1>(d, tv, sp, k, s);
+  return launch_tile_t<MODE, REC_GENERAL, 0>(d, tv, sp, k, s);
+}
+
+static cudaError_t launch_tile_stage(const DevView& d, const TileView& tv, const StageParams& sp, int k,
+                                     cudaStream_t s) {
+  if (sp.mode == MODE_SSP42) return launch_tile_mode<MODE_SSP42>(d, tv, sp, k, s);
+  if (sp.mode == MODE_SSP3) return launch_tile_mode<MODE_SSP3>(d, tv, sp, k, s);
+  return launch_tile_mode<MODE_RK>(d, tv, sp, k, s);
+}
+
+// opts every instantiation in to the shared memory of the plan's largest
+// tile; returns the bytes of one block (0: more than a block may have)
+static size_t tile_smem(int lmax, int gmax, int fmax) {
+  const size_t bytes = tile_smem_bytes(lmax, gmax, fmax);
+  int dev = 0, cap = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&cap, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess)
+    return 0;
+  if (bytes + 4 * 256 * sizeof(double) + 64 > (size_t)cap) return 0;
+  const int b = (int)bytes;
+  bool ok = true;
+#define FVS_TILE_ATTR(M)                                                                                           \
+  ok = ok && cudaFuncSetAttribute(k_tile_stage<M, REC_FIRST, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, b) == \
+                 cudaSuccess;                                                                                      \
+  ok = ok && cudaFuncSetAttribute(k_tile_stage<M, REC_SPEC, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, b) ==  \
+                 cudaSuccess;                                                                                      \
+  ok = ok && cudaFuncSetAttribute(k_tile_stage<M, REC_GENERAL, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,     \
+                                  b) == cudaSuccess;                                                               \
+  ok = ok && cudaFuncSetAttribute(k_tile_stage<M, REC_GENERAL, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,     \
+                                  b) == cudaSuccess
+  FVS_TILE_ATTR(MODE_SSP42);
+  FVS_TILE_ATTR(MODE_SSP3);
+  FVS_TILE_ATTR(MODE_RK);
+#undef FVS_TILE_ATTR
+  return ok ? bytes : 0;
+}
+#endif  // FVS_MIXED || FVS_DF
 
 // standalone compute_residual output: resid and ws_nrml
 __global__ void __launch_bounds__(256) k_residual_out(const DevView d) {

@@ -134,11 +134,13 @@ struct Layout {
 };
 
 // Appends one mesh (case index `cs`) to the layout.  fold_w: LSQ weights
-// multiplied into the coefficients (the FP64 and mixed kernels).
+// multiplied into the coefficients (the FP64 and mixed kernels).  order:
+// reference cell -> local device index (default: reverse Cuthill-McKee).
 template <typename T>
-int append_case(Layout<T>& L, const HostMesh& h, bool fold_w, int cs, std::string& err) {
+int append_case(Layout<T>& L, const HostMesh& h, bool fold_w, int cs, std::string& err,
+                const std::vector<int>* order = nullptr) {
   const int nc = h.nc, coff = L.nc, eoff = L.ne;
-  const std::vector<int> lperm = rcm_order(h);
+  const std::vector<int> lperm = order ? *order : rcm_order(h);
   std::vector<int> perm(nc), iperm(nc);
   for (int i = 0; i < nc; i++) {
     perm[i] = coff + lperm[i];

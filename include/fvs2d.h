@@ -224,6 +224,13 @@ int fvs_launches_per_step(const fvs_handle* h, int32_t* n);
 /* Device pointer of the conservative state (RCM order) and the permutation
  * old->new (host copy, 0-based) for callers that keep data on the device. */
 int fvs_device_state(fvs_handle* h, void** dptr);
+/* Host-only check of the fused stage's tile plan (no counterpart in the
+ * reference; no GPU needed): builds the plan a mixed or double-float handle
+ * would use for this mesh and checks every index its kernel derives from it.
+ * info[6] = (tiles, largest local cell count, largest gradient cell count,
+ * largest face count, 1 if every check holds, halo entries).  Returns
+ * FVS_ERR_MESH (message in fvs_last_error(NULL)) on the first violation. */
+int fvs_tile_plan_info(const fvs_mesh* mesh, const fvs_options* opt, int32_t* info);
 /* Check of the FP64 kernels' reciprocal and square root (no counterpart in
  * the reference): for n host values x (positive normal numbers), out
  * [n][5] = (the kernels' 1/x, IEEE 1/x, the kernels' 1/sqrt(x), the

@@ -26,9 +26,16 @@ def test_gradients_match_cpu_oracle(n, n_in, width, depth, n_out, engine):
     p = m.get_params()
     loss, g = m.loss_grad(x, y)
     ref_loss, ref_g = mlp_oracle.loss_grad(p, x.astype(np.float64), y.astype(np.float64), n_in, width, depth, n_out)
-    assert abs(loss - ref_loss) <= 1e-3 * abs(ref_loss)
+    # The oracle replays the BF16 roundings of the activations; only the FP32
+    # accumulation order differs.  Where an activation lies next to a BF16
+    # rounding boundary, that order decides its rounding, and one flip moves
+    # the activation by 2^-8 relative.  Measured on GB300 over these cases
+    # (both engines): loss 9.3e-6, gradient 1.3e-4 overall and 2.5e-4 for
+    # the worst layer (width 256, depth 4); without flips (width <= 48)
+    # ~1e-7.  Bars: 4-5x the measured worst case.
+    assert abs(loss - ref_loss) <= 5e-5 * abs(ref_loss)
     err = np.linalg.norm(g - ref_g) / np.linalg.norm(ref_g)
-    assert err < 1e-2, err
+    assert err < 5e-4, err
     # every layer's gradient, not only the largest
     off = 0
     dims_in = [n_in] + [width] * depth
@@ -36,7 +43,7 @@ def test_gradients_match_cpu_oracle(n, n_in, width, depth, n_out, engine):
     for i, o in zip(dims_in, dims_out):
         k = i * o + o
         e = np.linalg.norm(g[off:off + k] - ref_g[off:off + k]) / max(np.linalg.norm(ref_g[off:off + k]), 1e-30)
-        assert e < 3e-2, (i, o, e)
+        assert e < 1e-3, (i, o, e)
         off += k
 
 
