@@ -158,6 +158,27 @@ __device__ __forceinline__ float dabs_(float x) { return fabsf(x); }
 __device__ __forceinline__ double half(double x) { return 0.5 * x; }
 __device__ __forceinline__ float half(float x) { return 0.5f * x; }
 
+#if FVS_MIXED
+// FP32 limiter with every product and sum pinned (explicit multiply-adds),
+// so that the compiler's contraction choices cannot differ between the
+// kernels that inline it (the separate gradient kernel and the fused tile
+// stage give bit-identical limiter values)
+__device__ __forceinline__ float limiter_fn(int type, float a, float b, float eps2) {
+  if (type == FVS_LIM_VENK) {
+    const float num = __fmaf_rn(__fmul_rn(2.0f, b), a, __fmaf_rn(a, a, eps2));
+    const float den = __fadd_rn(__fmaf_rn(a, b, __fmaf_rn(a, a, __fmul_rn(2.0f, __fmul_rn(b, b)))), eps2);
+    return num / den;
+  }
+  if (type == FVS_LIM_BARTH) { const float q = a / b; return q < 1.0f ? q : 1.0f; }
+  const float num = __fmaf_rn(__fmaf_rn(a, a, eps2), b, __fmul_rn(__fmaf_rn(b, b, eps2), a));
+  const float den = __fmaf_rn(2.0f, eps2, __fmaf_rn(a, a, __fmul_rn(b, b)));
+  return (num / den) / __fadd_rn(b, eps2);
+}
+// a face value p + cx gx + cy gy with the same pinned sequence
+__device__ __forceinline__ float face_value(float p, float cx, float gx, float cy, float gy) {
+  return __fmaf_rn(cy, gy, __fmaf_rn(cx, gx, p));
+}
+#else
 // limiter, src/gradient_limiter.f90:103-134 (eps2 precomputed per cell)
 __device__ __forceinline__ T limiter_fn(int type, T a, T b, T eps2) {
   if (type == FVS_LIM_VENK) return ((a * a + eps2) + T(2) * b * a) / (a * a + T(2) * (b * b) + a * b + eps2);
@@ -165,6 +186,8 @@ __device__ __forceinline__ T limiter_fn(int type, T a, T b, T eps2) {
   T l = ((b * b + eps2) * a + (a * a + eps2) * b) / (a * a + b * b + T(2) * eps2);
   return l / (b + eps2);
 }
+__device__ __forceinline__ T face_value(T p, T cx, T gx, T cy, T gy) { return p + cx * gx + cy * gy; }
+#endif
 
 // flux_invscid_roe, src/flux_invscid.f90:37-136 (same operation order)
 __device__ __forceinline__ void roe_flux(T gamma, const T* pl, const T* pr, T nx, T ny, T* flux, T& ws_max) {
@@ -450,7 +473,7 @@ __device__ __forceinline__ void gradient_core(const DevView& d, int ic, const T*
 #pragma unroll
       for (int f = 0; f < 4; f++) {
         if (f >= nv) break;
-        const T pf = pc[v] + cp[f].x * gx[v] + cp[f].y * gy[v];
+        const T pf = face_value(pc[v], cp[f].x, gx[v], cp[f].y, gy[v]);
         const T dmax = pmax[v] - pc[v], dmin = pmin[v] - pc[v], diff = pf - pc[v];
         if (diff > T(0)) pe[f] = limiter_fn(d.limiter, dmax, diff, eps2);
         else if (diff < T(0)) pe[f] = limiter_fn(d.limiter, dmin, diff, eps2);

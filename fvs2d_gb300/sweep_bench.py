@@ -137,6 +137,56 @@ def run_airfoil(nw=512, nr=256, mach=0.8, aoa=1.25, drop=1e-10, switch=1e-5, max
     return out
 
 
+def run_airfoil_limited(nw=512, nr=256, mach=0.8, aoa=1.25, cfls=(1.25, 0.8), max_steps=50000, drop=1e-10,
+                        chunk=1000):
+    """The NACA0012 O-grid as configured: LSQ face-neighbour gradients with
+    the Venkatakrishnan limiter (K = 5, src/gradient_limiter.f90:113-117),
+    second-order reconstruction, steady SSP-RK(4,2) with local time steps,
+    on the FP64 drop-in path.  For each CFL: steps until every RMS(dU)
+    component falls to `drop` x its first-step value, the step cap, or the
+    first non-finite norm; the smallest RMS(dU_rho) ratio reached by 1k,
+    10k and all steps; and the wall time."""
+    from .options import Options
+    from .solver import FvsError, Solver
+    from .meshgen import naca0012_ogrid
+    mesh = naca0012_ogrid(nw, nr)
+    out = {"workload": f"NACA0012 O-grid {nw}x{nr} nodes, {mesh.ncells} cells, M {mach}, AoA {aoa} deg, steady "
+                       "SSP-RK(4,2), local dt, LSQ-fn + Venkatakrishnan K=5, second-order upwind, Roe, FP64",
+           "target": f"RMS(dU_k) <= {drop:g} x first-step RMS(dU_k), k = 1..4", "runs": []}
+    for cfl in cfls:
+        opt = Options(mach_inf=mach, aoa_inf_deg=aoa, steady=True, cfl=cfl, rk_nstages=4, rk_order=2, ssprk=True,
+                      grad_method=3, lsq_stencil="fn", limiter=1, reconst=2, dt=0.01, precision=PREC_FP64)
+        r = {"cfl": cfl}
+        t0 = time.perf_counter()
+        with Solver(mesh, opt) as s:
+            s.initialize_solution()
+            logs, done, status = [], 0, "step cap"
+            while done < max_steps:
+                n = min(chunk, max_steps - done)
+                try:
+                    log = s.time_integration(0.0, n)
+                except FvsError as e:
+                    status = f"non-finite: {e}"
+                    break
+                logs.append(log)
+                done += n
+                first = logs[0][0]
+                hit = np.nonzero(np.all(log <= drop * first[None, :], axis=1))[0]
+                if hit.size:
+                    done += int(hit[0]) + 1 - n
+                    status = "target reached"
+                    break
+        r["seconds"] = round(time.perf_counter() - t0, 2)
+        r["status"] = status
+        r["steps"] = int(done)
+        if logs:
+            rel = np.concatenate(logs)[:, 0] / logs[0][0][0]
+            r["min_rho_ratio"] = {str(k): float(rel[:k].min()) for k in (1000, 10000, len(rel)) if k <= len(rel)}
+            r["last_rho_ratio"] = float(rel[-1])
+        out["runs"].append(r)
+    return out
+
+
 def profile_batch(ncases=16, steps=400, chunk=200, fused=False):
     """A fixed amount of batched work for kernel profiling: the 16-case reduced
     sweep (261,780 cells), persistent launches of 256 threads, tiles of 1024
