@@ -29,11 +29,13 @@ UNITS = {
     "fvs_kern_fast.cu": ["-fmad=true"],
     "fvs_kern_mixed.cu": ["-fmad=true"],
     "fvs_kern_df.cu": ["-fmad=true"],
+    "fvs_kern_bounds.cu": ["-fmad=true"],
     "fvs_noalloc.cu": [],
     "fvs_batch.cu": [],
     "fvs_mlp.cu": [],
 }
-HEADERS = ["fvs_internal.hpp", "fvs_kernels.cuh", "fvs_layout.hpp", "df64.cuh", "fvs_tcgemm.cuh"]
+HEADERS = ["fvs_internal.hpp", "fvs_kernels.cuh", "fvs_layout.hpp", "fvs_tiles.hpp", "df64.cuh", "fp64_fast.cuh",
+           "fvs_tcgemm.cuh"]
 
 
 def nvcc() -> str:

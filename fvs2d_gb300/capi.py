@@ -19,8 +19,9 @@ FVS_ERR_NONFINITE = 4
 FVS_ERR_DIVERGED = 5
 FVS_ERR_TIMEOUT = 6
 FVS_ERR_NOMEM = 7
+FVS_ERR_BOUNDS = 8
 ERROR_NAMES = {0: "FVS_OK", 1: "FVS_ERR_INVALID", 2: "FVS_ERR_MESH", 3: "FVS_ERR_CUDA", 4: "FVS_ERR_NONFINITE",
-               5: "FVS_ERR_DIVERGED", 6: "FVS_ERR_TIMEOUT", 7: "FVS_ERR_NOMEM"}
+               5: "FVS_ERR_DIVERGED", 6: "FVS_ERR_TIMEOUT", 7: "FVS_ERR_NOMEM", 8: "FVS_ERR_BOUNDS"}
 
 PREC_FP64_STRICT = 0
 PREC_FP64 = 1
@@ -89,6 +90,7 @@ SIGNATURES = {
     "fvs_device_state": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
     "fvs_check_fp64_math": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p]),
     "fvs_tile_plan_info": (C.c_int, [C.POINTER(FvsMesh), C.POINTER(FvsOptions), C.c_void_p]),
+    "fvs_debug_set_gather": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32]),
     "fvs_batch_create": (C.c_int, [C.POINTER(FvsMesh), C.POINTER(FvsOptions), C.c_int32, C.c_int32, C.POINTER(C.c_void_p)]),
     "fvs_batch_destroy": (None, [C.c_void_p]),
     "fvs_batch_last_error": (C.c_char_p, [C.c_void_p]),

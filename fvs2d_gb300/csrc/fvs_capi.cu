@@ -142,6 +142,8 @@ struct fvs_handle {
   bool host_only = false;
   double* d_wall = nullptr;  // wall-load scratch, allocated on first use
   size_t wall_cap = 0;
+  // index-checking kernels (FVS2D_BOUNDS=1): their error word
+  bool bounds = false;
   // fused RK stage (mixed and double-float): cells in tile order, one
   // launch per stage (k_tile_stage)
   bool fused = false;
@@ -329,6 +331,21 @@ int check_launch(fvs_handle* H, const char* where) {
   return e == cudaSuccess ? FVS_OK : H->cuda_fail(e, where);
 }
 
+// index-checking handles: FVS_ERR_BOUNDS for a recorded violation (the word
+// is cleared, so later calls report later violations); call after the
+// stream has been synchronised
+int bounds_report(fvs_handle* H) {
+  if (!H->bounds) return FVS_OK;
+  int w[4];
+  cudaError_t e = cudaMemcpy(w, H->d.bounds_err, sizeof w, cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return H->cuda_fail(e, "bounds word download");
+  if (!w[0]) return FVS_OK;
+  static const char* site[] = {"?", "stencil cell", "edge left cell", "edge right cell", "gather slot"};
+  cudaMemset(H->d.bounds_err, 0, sizeof w);
+  return H->fail(FVS_ERR_BOUNDS, std::string("index-checking kernels: ") + site[(w[1] >= 1 && w[1] <= 4) ? w[1] : 0] +
+                                     " index " + std::to_string(w[2]) + " outside its array of " + std::to_string(w[3]));
+}
+
 // residual of the current device state at `time` (stage-free): fills d.resid, d.ws
 int device_residual(fvs_handle* H, double time) {
   NvtxRange nv("fvs residual (gradient, flux, gather)");
@@ -461,6 +478,11 @@ int fvs_create(const fvs_mesh* mesh, const fvs_options* opt, fvs_handle** out) {
   H->df = H->o.precision == FVS_PREC_FP64_DF;
   H->ks = H->o.precision == FVS_PREC_FP64_STRICT ? &kernels_fp64_strict()
           : H->mixed ? &kernels_mixed() : H->df ? &kernels_fp64_df() : &kernels_fp64_fast();
+  {
+    const char* e = std::getenv("FVS2D_BOUNDS");
+    H->bounds = H->o.precision == FVS_PREC_FP64 && e && e[0] == '1' && e[1] == 0;
+    if (H->bounds) H->ks = &kernels_fp64_bounds();
+  }
   cudaError_t e = cudaStreamCreateWithFlags(&H->stream, cudaStreamNonBlocking);
   if (e != cudaSuccess) { g_create_error = std::string("cudaStreamCreate: ") + cudaGetErrorString(e); return FVS_ERR_CUDA; }
   if (cudaMallocHost(&H->h_small, 64) != cudaSuccess) { g_create_error = "pinned allocation failed"; return FVS_ERR_NOMEM; }
@@ -488,6 +510,11 @@ int fvs_create(const fvs_mesh* mesh, const fvs_options* opt, fvs_handle** out) {
     rc = H->mixed ? build_device<float>(H.get()) : H->df ? build_device<df64>(H.get()) : build_device<double>(H.get());
   }
   if (rc) { g_create_error = H->err; return rc; }
+  if (H->bounds) {
+    void* p = nullptr;
+    if (!H->arena.alloc(p, 4 * sizeof(int))) { g_create_error = "bounds word allocation failed"; return FVS_ERR_NOMEM; }
+    d.bounds_err = static_cast<int*>(p);
+  }
   H->dt = H->o.dt;
   // steady runs start from dt_local = dt (src/runge_kutta.f90:73-76)
   {
@@ -604,7 +631,8 @@ int fvs_residual(fvs_handle* h, double time, double* resid, double* ws_nrml) {
   if (resid && (rc = state_out(h, h->d.resid, resid, 4))) return rc;
   if (ws_nrml && (rc = state_out(h, h->d.ws, ws_nrml, 1))) return rc;
   cudaError_t e = cudaStreamSynchronize(h->stream);
-  return e == cudaSuccess ? FVS_OK : h->cuda_fail(e, "residual");
+  if (e != cudaSuccess) return h->cuda_fail(e, "residual");
+  return bounds_report(h);
 }
 
 int fvs_get_gradient(fvs_handle* h, double* grad, double* phi) {
@@ -667,6 +695,7 @@ static int run_steps(fvs_handle* h, double t1, int nsteps, double* resnorm, floa
   }
   e = cudaStreamSynchronize(h->stream);
   if (e != cudaSuccess) return h->cuda_fail(e, "time integration");
+  if ((rc = bounds_report(h))) return rc;
   if (resnorm) {
     for (size_t i = 0; i < 4 * (size_t)nsteps; i++)
       if (!std::isfinite(resnorm[i])) return h->fail(FVS_ERR_NONFINITE, "residual norm is not finite at step " + std::to_string(i / 4 + 1));
@@ -866,6 +895,17 @@ int fvs_launches_per_step(const fvs_handle* h, int32_t* n) {
   if (!h || !n) return FVS_ERR_INVALID;
   *n = h->launches_per_step;
   return FVS_OK;
+}
+
+int fvs_debug_set_gather(fvs_handle* h, int32_t cell, int32_t entry, int32_t value) {
+  if (!h) return FVS_ERR_INVALID;
+  if (!h->bounds) return h->fail(FVS_ERR_INVALID, "fvs_debug_set_gather needs an index-checking handle (FVS2D_BOUNDS=1)");
+  if (cell < 1 || cell > h->hm.nc || entry < 0 || entry > 3) return h->fail(FVS_ERR_INVALID, "cell or entry out of range");
+  int* p = reinterpret_cast<int*>(const_cast<int4*>(h->d.cflist) + h->perm[cell - 1]) + entry;
+  // the kernels read the list from memory at every launch, so a captured
+  // step graph sees the new entry
+  cudaError_t e = cudaMemcpy(p, &value, sizeof value, cudaMemcpyHostToDevice);
+  return e == cudaSuccess ? FVS_OK : h->cuda_fail(e, "gather entry upload");
 }
 
 int fvs_tile_plan_info(const fvs_mesh* mesh, const fvs_options* opt, int32_t* info) {

@@ -129,6 +129,7 @@ struct DevView {
   double* partials = nullptr;     // [nblk_red] x 4
   double* norms = nullptr;        // [norm_cap] x 4
   int norm_cap = 0;
+  int* bounds_err = nullptr;      // [4] index-checking kernels: flag, site, index, extent
   int* stepctl = nullptr;         // [0] = steps done in this call
   double* tctl = nullptr;         // [0] = t1, [1] = told of the current step
   // scheme
@@ -282,5 +283,6 @@ const KernelSet& kernels_fp64_strict();
 const KernelSet& kernels_fp64_fast();
 const KernelSet& kernels_mixed();
 const KernelSet& kernels_fp64_df();
+const KernelSet& kernels_fp64_bounds();
 
 }  // namespace fvs

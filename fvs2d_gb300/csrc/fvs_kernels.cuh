@@ -27,6 +27,8 @@
 
 #include <cuda_runtime.h>
 
+#include <cstdlib>
+
 #include "df64.cuh"
 #include "fp64_fast.cuh"
 #include "fvs_internal.hpp"
@@ -36,12 +38,76 @@
 #endif
 // the FP64 build with multiply-add contraction (FVS_PREC_FP64)
 #define FVS_FP64_FAST (!FVS_STRICT && !FVS_MIXED && !FVS_DF)
+// the index-checking build (FVS2D_BOUNDS=1 handles): FP64 arithmetic with
+// every indirect index checked
+#ifndef FVS_BOUNDS
+#define FVS_BOUNDS 0
+#endif
 
 namespace fvs {
 namespace FVS_NS {
 
 using T = FVS_T;
 struct T2 { T x, y; };
+
+// Index check of the index-checking build: i must lie in [lo, hi).  On a
+// violation the first one is recorded in d.bounds_err (flag, site, index,
+// extent) and index 0 (a valid cell and edge slot) is used instead, so the
+// kernel carries on without touching memory outside the array.  Other builds
+// return i unchecked.
+enum : int { SITE_STENCIL = 1, SITE_EDGE_L = 2, SITE_EDGE_R = 3, SITE_GATHER = 4 };
+__device__ __forceinline__ int chk_idx(int* err, int i, int lo, int hi, int site) {
+#if FVS_BOUNDS
+  if (i < lo || i >= hi) {
+    if (atomicCAS(err, 0, 1) == 0) {
+      err[1] = site;
+      err[2] = i;
+      err[3] = hi;
+    }
+    return 0;
+  }
+#else
+  (void)err; (void)lo; (void)hi; (void)site;
+#endif
+  return i;
+}
+
+// Programmatic dependent launch.  The single-mesh step kernels are launched
+// with the programmatic stream serialization attribute (launch_k below), so
+// a kernel's blocks may be scheduled while its predecessor in the stream
+// finishes.  pdl_wait() blocks until the predecessor grid has completed and
+// its memory writes are visible; every kernel calls it before its first
+// global memory access, so results are unchanged.  pdl_trigger() right after
+// lets this grid's successor be launched once every block of this grid has
+// started.  Launched without the attribute, both return at once.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
+// programmatic dependent launch of the single-mesh step kernels (see
+// pdl_wait); FVS2D_PDL=0 in the environment launches them plainly
+static bool pdl_enabled() {
+  static const bool on = [] {
+    const char* e = std::getenv("FVS2D_PDL");
+    return !(e && e[0] == '0' && e[1] == 0);
+  }();
+  return on;
+}
+
+template <typename... KArgs, typename... Args>
+static void launch_k(void (*kern)(KArgs...), unsigned grid, unsigned block, size_t smem, cudaStream_t s,
+                     Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(block);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = pdl_enabled() ? 1 : 0;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, kern, args...);
+}
 
 __device__ __forceinline__ void ld4(const double* __restrict__ p, int i, double* o) {
   const double2* q = reinterpret_cast<const double2*>(p) + 2 * (size_t)i;
@@ -494,7 +560,9 @@ __device__ __forceinline__ void gradient_item(const DevView& d, int ic) {
   const T* P = static_cast<const T*>(d.Pv);
   T pc[4], gx[4], gy[4], ph;
   ldc4<COH>(P, ic, pc);
-  gradient_core<METHOD, LIM>(d, ic, pc, [&](int k, T* pj) { ldc4<COH>(P, d.st_cell[k], pj); }, gx, gy, ph);
+  gradient_core<METHOD, LIM>(
+      d, ic, pc, [&](int k, T* pj) { ldc4<COH>(P, chk_idx(d.bounds_err, d.st_cell[k], 0, d.nc, SITE_STENCIL), pj); },
+      gx, gy, ph);
   st4(static_cast<T*>(d.Gx), ic, gx);
   st4(static_cast<T*>(d.Gy), ic, gy);
   if (LIM) static_cast<T*>(d.phi)[ic] = ph;
@@ -502,6 +570,8 @@ __device__ __forceinline__ void gradient_item(const DevView& d, int ic) {
 
 template <int METHOD, int LIM>
 __global__ void __launch_bounds__(256) k_gradient(const DevView d) {
+  pdl_wait();
+  pdl_trigger();
   const int ic = blockIdx.x * blockDim.x + threadIdx.x;
   if (ic < d.nc) gradient_item<METHOD, LIM, false>(d, ic);
 }
@@ -671,7 +741,9 @@ __device__ __forceinline__ void flux_item(const DevView& d, int e, double time) 
   const T* GX = static_cast<const T*>(d.Gx);
   const T* GY = static_cast<const T*>(d.Gy);
   const T* PH = static_cast<const T*>(d.phi);
-  const int2 lr = d.ecell[e];
+  int2 lr = d.ecell[e];
+  lr.x = chk_idx(d.bounds_err, lr.x, 0, d.nc, SITE_EDGE_L);
+  lr.y = chk_idx(d.bounds_err, lr.y, -1, d.nc, SITE_EDGE_R);
   const T2 n = ld2(d.enrm, e);
   const T af = static_cast<const T*>(d.earea)[e];
   const bool interior = lr.y >= 0;
@@ -741,6 +813,8 @@ __device__ __forceinline__ void flux_range(const DevView& d, int b, int end, int
 
 template <int REC>
 __global__ void __launch_bounds__(256) k_flux(const DevView d, double dts) {
+  pdl_wait();
+  pdl_trigger();
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
   if (e < d.nedge) flux_item<REC, false>(d, e, d.tctl[1] + dts);
 }
@@ -821,7 +895,7 @@ __device__ __forceinline__ void cell_residual(const DevView& d, int ic, double* 
 template <bool WS, bool COH>
 __device__ __forceinline__ void gather_slot(const DevView& d, int s, double* r, double& ws) {
   if (s == 0) return;
-  const int idx = (s > 0 ? s : -s) - 1;
+  const int idx = chk_idx(d.bounds_err, (s > 0 ? s : -s) - 1, 0, d.nedge, SITE_GATHER);
   double f[4];
   ldc4<COH>(static_cast<const double*>(d.eflux), idx, f);
   if (s > 0) {
@@ -1155,6 +1229,8 @@ __device__ __forceinline__ void stage_norms(const DevView& d, const double* d2) 
 
 template <int MODE>
 __global__ void __launch_bounds__(256) k_update(const DevView d, const StageParams sp) {
+  pdl_wait();
+  pdl_trigger();
   const int ic = blockIdx.x * blockDim.x + threadIdx.x;
   double d2[4] = {0.0, 0.0, 0.0, 0.0};
   if (ic < d.nc) update_item<MODE, false>(d, sp, ic, d2);
@@ -1189,6 +1265,8 @@ static size_t tile_smem_bytes(int lmax, int gmax, int fmax) {
 template <int MODE, int REC, int LIM>
 __global__ void __launch_bounds__(256) k_tile_stage(const DevView d, const TileView tv, const StageParams sp, int kin,
                                                    int kout) {
+  pdl_wait();
+  pdl_trigger();
   extern __shared__ __align__(16) unsigned char tile_shm[];
   const int t = blockIdx.x, tid = threadIdx.x, nthr = blockDim.x;
   const int b = tv.c0[t], n = tv.c0[t + 1] - b;
@@ -1280,7 +1358,8 @@ __global__ void __launch_bounds__(256) k_tile_stage(const DevView d, const TileV
 
 template <int MODE, int REC, int LIM>
 static cudaError_t launch_tile_t(const DevView& d, const TileView& tv, const StageParams& sp, int k, cudaStream_t s) {
-  k_tile_stage<MODE, REC, LIM><<<tv.ntiles, 256, tv.smem_bytes, s>>>(d, tv, sp, k % tv.nbuf, (k + 1) % tv.nbuf);
+  launch_k(k_tile_stage<MODE, REC, LIM>, (unsigned)tv.ntiles, 256, tv.smem_bytes, s, d, tv, sp, k % tv.nbuf,
+           (k + 1) % tv.nbuf);
   return cudaGetLastError();
 }
 
@@ -1331,6 +1410,8 @@ static size_t tile_smem(int lmax, int gmax, int fmax) {
 
 // standalone compute_residual output: resid and ws_nrml
 __global__ void __launch_bounds__(256) k_residual_out(const DevView d) {
+  pdl_wait();
+  pdl_trigger();
   const int ic = blockIdx.x * blockDim.x + threadIdx.x;
   if (ic >= d.nc) return;
   double res[4], ws;
@@ -1340,6 +1421,8 @@ __global__ void __launch_bounds__(256) k_residual_out(const DevView d) {
 }
 
 __global__ void __launch_bounds__(256) k_cvar2pvar(const DevView d) {
+  pdl_wait();
+  pdl_trigger();
   const int ic = blockIdx.x * blockDim.x + threadIdx.x;
   if (ic >= d.nc) return;
   double u[4];
@@ -1351,6 +1434,8 @@ __global__ void __launch_bounds__(256) k_cvar2pvar(const DevView d) {
 
 // told = t1 + (istep-1)*dt, src/runge_kutta.f90:207-208
 __global__ void k_begin_step(const DevView d) {
+  pdl_wait();
+  pdl_trigger();
   const int istep = d.stepctl[0] + 1;
   d.tctl[1] = d.tctl[0] + double(istep - 1) * d.dt;
 }
@@ -1752,8 +1837,9 @@ static cudaError_t launch_tiled_step(const DevView& d, const PersistPlan& p, int
 // ---------------------------------------------------------------------------
 static inline unsigned grid_of(int n) { return (unsigned)((n + 255) / 256); }
 
-static void launch_begin_step(const DevView& d, cudaStream_t s) { k_begin_step<<<1, 1, 0, s>>>(d); }
-static void launch_cvar2pvar(const DevView& d, cudaStream_t s) { k_cvar2pvar<<<grid_of(d.nc), 256, 0, s>>>(d); }
+
+static void launch_begin_step(const DevView& d, cudaStream_t s) { launch_k(k_begin_step, 1, 1, 0, s, d); }
+static void launch_cvar2pvar(const DevView& d, cudaStream_t s) { launch_k(k_cvar2pvar, grid_of(d.nc), 256, 0, s, d); }
 
 static void launch_gradient(const DevView& d, cudaStream_t s) {
   if (d.first_order) return;
@@ -1761,31 +1847,31 @@ static void launch_gradient(const DevView& d, cudaStream_t s) {
   const bool lim = d.limiter != FVS_LIM_NONE;
   switch (d.grad_method) {
     case FVS_GRAD_LSQ:
-      if (lim) k_gradient<FVS_GRAD_LSQ, 1><<<g, 256, 0, s>>>(d);
-      else k_gradient<FVS_GRAD_LSQ, 0><<<g, 256, 0, s>>>(d);
+      if (lim) launch_k(k_gradient<FVS_GRAD_LSQ, 1>, g, 256, 0, s, d);
+      else launch_k(k_gradient<FVS_GRAD_LSQ, 0>, g, 256, 0, s, d);
       break;
-    case FVS_GRAD_GGCB: k_gradient<FVS_GRAD_GGCB, 0><<<g, 256, 0, s>>>(d); break;
-    default: k_gradient<FVS_GRAD_GGNB, 0><<<g, 256, 0, s>>>(d); break;
+    case FVS_GRAD_GGCB: launch_k(k_gradient<FVS_GRAD_GGCB, 0>, g, 256, 0, s, d); break;
+    default: launch_k(k_gradient<FVS_GRAD_GGNB, 0>, g, 256, 0, s, d); break;
   }
 }
 
 static void launch_flux(const DevView& d, double dts, cudaStream_t s) {
   const bool spec = !FVS_STRICT && d.khalf == 0.0 && d.omk == 1.0 && d.limiter == FVS_LIM_NONE && !d.first_order;
-  if (d.first_order) k_flux<REC_FIRST><<<grid_of(d.nedge), 256, 0, s>>>(d, dts);
-  else if (spec) k_flux<REC_SPEC><<<grid_of(d.nedge), 256, 0, s>>>(d, dts);
-  else k_flux<REC_GENERAL><<<grid_of(d.nedge), 256, 0, s>>>(d, dts);
+  if (d.first_order) launch_k(k_flux<REC_FIRST>, grid_of(d.nedge), 256, 0, s, d, dts);
+  else if (spec) launch_k(k_flux<REC_SPEC>, grid_of(d.nedge), 256, 0, s, d, dts);
+  else launch_k(k_flux<REC_GENERAL>, grid_of(d.nedge), 256, 0, s, d, dts);
 }
 
 static void launch_update(const DevView& d, const StageParams& sp, cudaStream_t s) {
   const unsigned g = grid_of(d.nc);
   switch (sp.mode) {
-    case MODE_SSP42: k_update<MODE_SSP42><<<g, 256, 0, s>>>(d, sp); break;
-    case MODE_SSP3: k_update<MODE_SSP3><<<g, 256, 0, s>>>(d, sp); break;
-    default: k_update<MODE_RK><<<g, 256, 0, s>>>(d, sp); break;
+    case MODE_SSP42: launch_k(k_update<MODE_SSP42>, g, 256, 0, s, d, sp); break;
+    case MODE_SSP3: launch_k(k_update<MODE_SSP3>, g, 256, 0, s, d, sp); break;
+    default: launch_k(k_update<MODE_RK>, g, 256, 0, s, d, sp); break;
   }
 }
 
-static void launch_residual_out(const DevView& d, cudaStream_t s) { k_residual_out<<<grid_of(d.nc), 256, 0, s>>>(d); }
+static void launch_residual_out(const DevView& d, cudaStream_t s) { launch_k(k_residual_out, grid_of(d.nc), 256, 0, s, d); }
 
 #if FVS_MIXED
 // ---------------------------------------------------------------------------

@@ -42,6 +42,7 @@ extern "C" {
 #define FVS_ERR_DIVERGED  5  /* residual norm grew past options.diverge_factor   */
 #define FVS_ERR_TIMEOUT   6  /* a bounded device-side wait expired               */
 #define FVS_ERR_NOMEM     7  /* device or host allocation failed                 */
+#define FVS_ERR_BOUNDS    8  /* index-checking kernels met an out-of-range index */
 
 /* ---- boundary types (src/residual.f90:194-221; .bc strings) ------------ */
 #define FVS_BC_FREESTREAM 1  /* 'freestream'  */
@@ -224,6 +225,19 @@ int fvs_launches_per_step(const fvs_handle* h, int32_t* n);
 /* Device pointer of the conservative state (RCM order) and the permutation
  * old->new (host copy, 0-based) for callers that keep data on the device. */
 int fvs_device_state(fvs_handle* h, void** dptr);
+/* Index-checking kernels (no counterpart in the reference, which has no
+ * sanitizer either).  With the environment variable FVS2D_BOUNDS=1 at
+ * fvs_create, an FVS_PREC_FP64 handle runs kernels built with every
+ * indirect index (stencil cells, edge cells, gather slots) checked against
+ * its array's extent.  A kernel that meets a violation records the first one
+ * in a device word, substitutes index 0 and carries on (no trap, no fault);
+ * fvs_time_integration, fvs_steps_device and fvs_residual then return
+ * FVS_ERR_BOUNDS with the site, index and extent in fvs_last_error.  The
+ * arithmetic is the FP64 handle's, so results are bit-identical to it.
+ * fvs_debug_set_gather writes one entry of a cell's gather list (cell
+ * 1-based, entry 0..3, value: signed 1-based edge slot or 0) and is refused
+ * except on such a handle: it exists to show that the checks fire. */
+int fvs_debug_set_gather(fvs_handle* h, int32_t cell, int32_t entry, int32_t value);
 /* Host-only check of the fused stage's tile plan (no counterpart in the
  * reference; no GPU needed): builds the plan a mixed or double-float handle
  * would use for this mesh and checks every index its kernel derives from it.
