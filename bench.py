@@ -448,13 +448,15 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=12.0)
     ap.add_argument("--no-time-to-drop", dest="time_to_drop", action="store_false",
                     help="skip the time-to-1e-10-drop measurement on the NACA0012 O-grid (about 45 s)")
-    ap.add_argument("--workload", default="vortex", choices=["vortex", "sweep", "airfoil", "airfoil-limited",
-                                                             "vortex-period"],
+    ap.add_argument("--workload", default="vortex", choices=["vortex", "sweep", "sweep-256", "airfoil",
+                                                             "airfoil-limited", "vortex-period"],
                     help="vortex: the 1,048,576-cell throughput case (default); sweep: time to a 1e-10 drop on an "
                          "airfoil sweep, plain FP64 vs batched ladder vs learned warm start; airfoil: time to a "
                          "1e-10 drop on the 261,120-cell NACA0012 O-grid, plain FP64 vs the ladder; airfoil-limited: "
                          "the same O-grid with the configured second-order Venkatakrishnan scheme, FP64, CFL 1.25 "
-                         "and 0.8, up to 50,000 steps; vortex-period: "
+                         "and 0.8, up to 50,000 steps; sweep-256: 256 held-out full-size cases, batched ladder "
+                         "from the free stream and from the learned start (network trained on 256 other cases, "
+                         "learning curve), plain FP64 on a 32-case subset; vortex-period: "
                          "errors of the arithmetic modes after one vortex period at 1,048,576 cells")
     ap.add_argument("--n-train", type=int, default=96)
     ap.add_argument("--n-test", type=int, default=24)
@@ -462,7 +464,7 @@ def main():
                     help="sweep meshes from the full distribution (64-512 wall x 32-256 radial nodes) instead of "
                          "64-192 x 32-96")
     args = ap.parse_args()
-    if args.workload in ("sweep", "airfoil", "airfoil-limited", "vortex-period"):
+    if args.workload in ("sweep", "sweep-256", "airfoil", "airfoil-limited", "vortex-period"):
         from fvs2d_gb300 import _build, accuracy, sweep_bench
         _build.build()
         clk = clock_sampler(int(os.environ.get("LOCAL_RANK", "0")))
@@ -471,6 +473,8 @@ def main():
         elif args.workload == "sweep":
             sizes = dict(wall=(64, 512), radial=(32, 256), race=False) if args.full_size else {}
             out = sweep_bench.run(args.n_train, args.n_test, **sizes)
+        elif args.workload == "sweep-256":
+            out = sweep_bench.run_scaled()
         elif args.workload == "airfoil-limited":
             out = sweep_bench.run_airfoil_limited()
         else:

@@ -216,6 +216,28 @@ int build_tiles(fvs_handle* H, const Layout<T>& L, const std::vector<int>& tile_
             A.upload(f0, P.f0) && A.upload(face, P.face) && A.upload(flr, P.flr) && A.upload(lcf, P.lcf);
   tv.c0 = c0; tv.h0 = h0; tv.nh1 = nh1; tv.halo = halo; tv.g0 = g0; tv.lsp = lsp; tv.s0 = s0; tv.lst = lst;
   tv.f0 = f0; tv.face = face; tv.flr = flr; tv.lcf = lcf;
+  // tile-major face records and gradient-cell records
+  std::vector<T> fgeo(8 * P.face.size(), T(0));
+  for (size_t f = 0; f < P.face.size(); f++) {
+    const int e = P.face[f];
+    T* g = &fgeo[8 * f];
+    g[0] = L.enrm[2 * (size_t)e]; g[1] = L.enrm[2 * (size_t)e + 1]; g[2] = L.earea[e];
+    g[3] = L.edL[2 * (size_t)e]; g[4] = L.edL[2 * (size_t)e + 1];
+    g[5] = L.edR[2 * (size_t)e]; g[6] = L.edR[2 * (size_t)e + 1];
+  }
+  std::vector<int2> gcell(P.lsp.size(), make_int2(0, 0));
+  for (int t = 0; t < P.ntiles; t++) {
+    const int b = P.c0[t], n = P.c0[t + 1] - b, ng = P.g0[t + 1] - P.g0[t] - 1;
+    for (int i = 0; i < ng; i++) {
+      const int gid = i < n ? b + i : P.halo[P.h0[t] + i - n];
+      gcell[P.g0[t] + i] = make_int2(gid, L.st_ptr[gid]);
+    }
+  }
+  T* dfgeo;
+  int2* dgcell;
+  up = up && A.upload(dfgeo, fgeo) && A.upload(dgcell, gcell);
+  tv.fgeo = dfgeo;
+  tv.gcell = dgcell;
   tv.nbuf = H->o.rk_nstages % 2 == 0 ? 2 : 3;
   tv.Pbuf[0] = H->d.Pv;
   for (int k = 1; k < tv.nbuf && up; k++) up = A.alloc(tv.Pbuf[k], sizeof(T) * 4 * (size_t)L.nc);

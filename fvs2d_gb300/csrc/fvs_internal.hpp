@@ -178,6 +178,8 @@ struct TileView {
   const int* face = nullptr;
   const uint32_t* flr = nullptr;
   const int2* lcf = nullptr;
+  const void* fgeo = nullptr;   // per tile face, 8 T: nx, ny, length, xf-xcL, yf-ycL, xf-xcR, yf-ycR, 0
+  const int2* gcell = nullptr;  // per gradient cell (lsp layout): device cell, first global stencil entry
   void* Pbuf[3] = {nullptr, nullptr, nullptr};
   int nbuf = 2;
   size_t smem_bytes = 0;  // dynamic shared memory of one block

@@ -681,9 +681,9 @@ __device__ __forceinline__ void flux_finish(const DevView& d, int e, const T* pf
 // state.  REC_FIRST reads no gradient; REC_SPEC no limiter value.  Shared by
 // the edge-flux kernel and the fused tile stage: the same arithmetic.
 template <int REC>
-__device__ __forceinline__ void face_states(const DevView& d, int e, bool interior, double time, T2 n, const T* pl,
-                                            const T* gxl, const T* gyl, T phiL, const T* pr, const T* gxr,
-                                            const T* gyr, T phiR, T* pfL, T* pfR) {
+__device__ __forceinline__ void face_states(const DevView& d, int e, bool interior, double time, T2 n, T2 dl, T2 dr,
+                                            const T* pl, const T* gxl, const T* gyl, T phiL, const T* pr,
+                                            const T* gxr, const T* gyr, T phiR, T* pfL, T* pfR) {
   constexpr bool SPEC = REC == REC_SPEC;
   if (REC == REC_FIRST) {
 #pragma unroll
@@ -697,10 +697,8 @@ __device__ __forceinline__ void face_states(const DevView& d, int e, bool interi
     }
     return;
   }
-  const T2 dl = ld2(d.edL, e);
   if (interior) {
     // src/residual.f90:83-92
-    const T2 dr = ld2(d.edR, e);
     if (SPEC) {
 #pragma unroll
       for (int v = 0; v < 4; v++) {
@@ -763,7 +761,12 @@ __device__ __forceinline__ void flux_item(const DevView& d, int e, double time) 
       if (!SPEC) phiR = ldc1<COH>(PH, lr.y);
     }
   }
-  face_states<REC>(d, e, interior, time, n, pl, gxl, gyl, phiL, pr, gxr, gyr, phiR, pfL, pfR);
+  T2 dl = {T(0), T(0)}, dr = {T(0), T(0)};
+  if (REC != REC_FIRST) {
+    dl = ld2(d.edL, e);
+    if (interior) dr = ld2(d.edR, e);
+  }
+  face_states<REC>(d, e, interior, time, n, dl, dr, pl, gxl, gyl, phiL, pr, gxr, gyr, phiR, pfL, pfR);
   flux_finish(d, e, pfL, pfR, n, af);
 }
 
@@ -1278,17 +1281,31 @@ __global__ void __launch_bounds__(256) k_tile_stage(const DevView d, const TileV
   T* sF = sPh + tv.gmax;
   const T* Pin = static_cast<const T*>(tv.Pbuf[kin]);
   T* Pout = static_cast<T*>(tv.Pbuf[kout]);
-  // 1. primitives
-  for (int i = tid; i < nl; i += nthr) ld4(Pin, i < n ? b + i : tv.halo[hb + i - n], sP + 4 * i);
+  // 1. primitives, two cells per pass (both loads in flight together)
+  for (int i0 = tid; i0 < nl; i0 += 2 * nthr) {
+    const int i1 = i0 + nthr;
+    const int g0 = i0 < n ? b + i0 : tv.halo[hb + i0 - n];
+    const int g1 = i1 < n ? b + i1 : (i1 < nl ? tv.halo[hb + i1 - n] : g0);
+    T v0[4], v1[4];
+    ld4(Pin, g0, v0);
+    ld4(Pin, g1, v1);
+#pragma unroll
+    for (int v = 0; v < 4; v++) sP[4 * i0 + v] = v0[v];
+    if (i1 < nl)
+#pragma unroll
+      for (int v = 0; v < 4; v++) sP[4 * i1 + v] = v1[v];
+  }
   __syncthreads();
-  // 2. gradients of the tile and halo1 cells
+  // 2. gradients of the tile and halo1 cells; each cell's record holds its
+  //    device index and the start of its global stencil entries
   if (REC != REC_FIRST) {
     const uint16_t* lst = tv.lst + tv.s0[t];
     const int* lsp = tv.lsp + tv.g0[t];
+    const int2* gcr = tv.gcell + tv.g0[t];
     for (int i = tid; i < ng; i += nthr) {
-      const int gid = i < n ? b + i : tv.halo[hb + i - n];
+      const int2 gc = gcr[i];
+      const int gid = gc.x, kb = gc.y;
       const uint16_t* L = lst + lsp[i];
-      const int kb = d.st_ptr[gid];
       auto load = [&](int k, T* pj) {
         const T* q = sP + 4 * (int)L[k - kb];
 #pragma unroll
@@ -1310,18 +1327,25 @@ __global__ void __launch_bounds__(256) k_tile_stage(const DevView d, const TileV
   // 3. face fluxes
   const double time = d.tctl[1] + sp.dts;
   const int fb = tv.f0[t], nf = tv.f0[t + 1] - fb;
+  const T* fg = static_cast<const T*>(tv.fgeo) + 8 * (size_t)fb;
   for (int f = tid; f < nf; f += nthr) {
-    const int e = tv.face[fb + f];
+    // the face's record: normal, length, the two centre-to-face offsets
+    // (coalesced: the tile's faces are stored one after the other)
     const uint32_t lr = tv.flr[fb + f];
+    T g[8];
+    ld4(fg, 2 * f, g);
+    ld4(fg, 2 * f + 1, g + 4);
     const int l = (int)(lr & 0xFFFFu), rr = (int)(lr >> 16);
     const bool interior = rr != 0xFFFF;
     const int r = interior ? rr : l;  // a boundary slot reads no right cell
-    const T2 nn = ld2(d.enrm, e);
-    const T af = static_cast<const T*>(d.earea)[e];
+    const int e = interior ? -1 : tv.face[fb + f];  // the slot's boundary record
+    const T2 nn = {g[0], g[1]};
+    const T af = g[2];
+    const T2 dl = {g[3], g[4]}, dr = {g[5], g[6]};
     T pfL[4], pfR[4], flux[4], wsa;
     const T phiL = REC == REC_GENERAL ? sPh[l] : T(1), phiR = REC == REC_GENERAL ? sPh[r] : T(1);
-    face_states<REC>(d, e, interior, time, nn, sP + 4 * l, sGx + 4 * l, sGy + 4 * l, phiL, sP + 4 * r, sGx + 4 * r,
-                     sGy + 4 * r, phiR, pfL, pfR);
+    face_states<REC>(d, e, interior, time, nn, dl, dr, sP + 4 * l, sGx + 4 * l, sGy + 4 * l, phiL, sP + 4 * r,
+                     sGx + 4 * r, sGy + 4 * r, phiR, pfL, pfR);
     flux_eval(d, pfL, pfR, nn, af, flux, wsa);
 #pragma unroll
     for (int v = 0; v < 4; v++) sF[5 * f + v] = flux[v];

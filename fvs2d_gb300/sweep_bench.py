@@ -108,6 +108,98 @@ def run(n_train=96, n_test=24, wall=(64, 192), radial=(32, 96), max_steps=400000
     return out
 
 
+def run_scaled(n_train=256, n_test=256, n_plain=32, curve=(32, 64, 128, 256), wall=(64, 512), radial=(32, 256),
+               max_steps=400000, epochs=30, seed_train=5, seed_test=6, drop=1e-10, switch=1e-5):
+    """The sweep at the stated scale: n_test held-out cases of the full
+    distribution (W 64-512, R 32-256: ~21M cells for 256 cases) solved by the
+    batched ladder from the free stream and from the learned start, the
+    network trained on the converged solutions of n_train other cases, with
+    a learning curve (surrogate error on the held-out cases for networks
+    trained on the first m training solutions).  The plain FP64 path (one
+    Solver per case, ~40 min for 256 cases) runs on the first n_plain
+    held-out cases, and both batched forms are timed on that subset too."""
+    out = {"distribution": {"wall": wall, "radial": radial, "mach": [0.3, 0.85], "aoa_deg": [-2, 4],
+                            "n_train": n_train, "n_test": n_test, "n_plain_subset": n_plain,
+                            "seeds": [seed_train, seed_test]},
+           "scheme": "steady SSP-RK(4,2), local dt CFL 1.25, first-order Roe, slip wall + free stream",
+           "target": f"RMS(dU_k) <= {drop:g} x first-step RMS(dU_k) of a free-stream start, k = 1..4"}
+    opts = lambda cs: [sweep.case_options(c, PREC_MIXED) for c in cs]  # noqa: E731
+    # ---- training solutions
+    train = sweep.draw_cases(n_train, seed_train, wall, radial)
+    tm = [c.mesh() for c in train]
+    lv_tr = reference_levels(train, tm)
+    st_tr, t1, t2, t_tr, _ = solve_ladder(tm, opts(train), lv_tr, switch, drop, max_steps)
+    out["training_solve"] = {"cells": int(sum(m.ncells for m in tm)), "seconds": round(t_tr, 2),
+                             "steps_total": int((t1 + t2).sum())}
+    # ---- held-out sweep from the free stream
+    test = sweep.draw_cases(n_test, seed_test, wall, radial)
+    meshes = [c.mesh() for c in test]
+    levels = reference_levels(test, meshes)
+    st_b, b1, b2, t_b, ph_b = solve_ladder(meshes, opts(test), levels, switch, drop, max_steps)
+    fs = [sweep.free_stream_state(c, m.ncells) for c, m in zip(test, meshes)]
+
+    def rel_err(a, b):
+        e_inf = [float(np.abs(x - y).max() / np.abs(y).max()) for x, y in zip(a, b)]
+        e_l2 = [float(np.sqrt(((x - y) ** 2).mean() / (y ** 2).mean())) for x, y in zip(a, b)]
+        return e_inf, e_l2
+
+    fs_inf, fs_l2 = rel_err(fs, st_b)
+    # ---- learning curve
+    rows, ws = [], None
+    for m in curve:
+        if m > n_train:
+            continue
+        X, Y = build_dataset(train[:m], st_tr[:m])
+        t0 = time.perf_counter()
+        ws = WarmStart(width=256, depth=4, seed=1)
+        losses = ws.fit(X, Y, epochs=epochs, batch=4096, lr=1e-3, seed=2)
+        t_fit = time.perf_counter() - t0
+        starts = [ws.predict_state(c, mm) for c, mm in zip(test, meshes)]
+        e_inf, e_l2 = rel_err(starts, st_b)
+        rows.append({"train_solutions": m, "samples": int(X.shape[0]), "train_seconds": round(t_fit, 2),
+                     "loss_first_last": [float(losses[0]), float(losses[-1])],
+                     "surrogate_l2_median": float(np.median(e_l2)), "surrogate_linf_median": float(np.median(e_inf))})
+    out["learning_curve"] = {"rows": rows, "free_stream_l2_median": float(np.median(fs_l2)),
+                             "free_stream_linf_median": float(np.median(fs_inf))}
+    # ---- held-out sweep from the learned start (largest network)
+    starts = [ws.predict_state(c, mm) for c, mm in zip(test, meshes)]
+    st_l, l1, l2, t_l, ph_l = solve_ladder(meshes, opts(test), levels, switch, drop, max_steps, starts=starts)
+    l_inf, _ = rel_err(st_l, st_b)
+    steps_b, steps_l = b1 + b2, l1 + l2
+    out["all_cases"] = {
+        "cells": int(sum(m.ncells for m in meshes)),
+        "batched_ladder": {"seconds": round(t_b, 2), "steps_total": int(steps_b.sum()),
+                           "phase_seconds": {k: round(v, 2) for k, v in ph_b.items()}},
+        "learned_batched_ladder": {"seconds": round(t_l, 2), "steps_total": int(steps_l.sum()),
+                                   "phase_seconds": {k: round(v, 2) for k, v in ph_l.items()}},
+        "learned_vs_free_stream": {"wall_time_ratio": round(t_l / t_b, 3),
+                                   "steps_ratio": round(float(steps_l.sum() / steps_b.sum()), 4),
+                                   "cases_with_fewer_steps": int((steps_l < steps_b).sum()),
+                                   "median_case_steps_ratio": float(np.median(steps_l / steps_b))},
+        "linf_learned_vs_free_stream": {"max": float(max(l_inf)), "cases_le_1e-6": int(sum(e <= 1e-6 for e in l_inf))},
+    }
+    # ---- plain FP64 on the subset, both batched forms on the same subset
+    sub = slice(0, min(n_plain, n_test))
+    plain_states = []
+    steps_p, t_p, _ = sweep.run_plain(test[sub], PREC_FP64, max_steps, drop, ref_levels=levels[sub], check_every=500,
+                                      states=plain_states, meshes=meshes[sub])
+    sb, s1, s2, t_sb, _ = solve_ladder(meshes[sub], opts(test[sub]), levels[sub], switch, drop, max_steps)
+    sl, u1, u2, t_sl, _ = solve_ladder(meshes[sub], opts(test[sub]), levels[sub], switch, drop, max_steps,
+                                       starts=starts[sub])
+    b_inf, _ = rel_err(sb, plain_states)
+    lp_inf, _ = rel_err(sl, plain_states)
+    out["plain_subset"] = {
+        "cases": len(plain_states), "cells": int(sum(m.ncells for m in meshes[sub])),
+        "plain_fp64": {"seconds": round(t_p, 2), "steps_total": int(steps_p.sum())},
+        "batched_ladder": {"seconds": round(t_sb, 2), "steps_total": int((s1 + s2).sum())},
+        "learned_batched_ladder": {"seconds": round(t_sl, 2), "steps_total": int((u1 + u2).sum())},
+        "speedup_batched": round(t_p / t_sb, 2), "speedup_learned": round(t_p / t_sl, 2),
+        "linf_vs_plain_batched": {"max": float(max(b_inf)), "cases_le_1e-6": int(sum(e <= 1e-6 for e in b_inf))},
+        "linf_vs_plain_learned": {"max": float(max(lp_inf)), "cases_le_1e-6": int(sum(e <= 1e-6 for e in lp_inf))},
+    }
+    return out
+
+
 def run_airfoil(nw=512, nr=256, mach=0.8, aoa=1.25, drop=1e-10, switch=1e-5, max_steps=400000):
     """Steady transonic NACA0012 O-grid (512 x 256 nodes, 261,120 cells,
     M 0.8, 1.25 deg) to a 1e-10 drop of every RMS(dU) component: the plain
