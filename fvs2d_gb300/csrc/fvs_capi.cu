@@ -197,6 +197,7 @@ int build_tiles(fvs_handle* H, const Layout<T>& L, const std::vector<int>& tile_
   std::string err;
   int rc = build_tile_plan(tile_start, L.ecell, L.cf, L.st_ptr, L.st_cell, P, err);
   if (rc) return H->fail(rc, err);
+  P.tile_cells = tile_cells_setting();
   err = check_tile_plan(P, L.nc, L.ne, L.ecell, L.cf, L.st_ptr);
   if (!err.empty()) return H->fail(FVS_ERR_MESH, "tile plan: " + err);
   TileView& tv = H->tv;
@@ -238,6 +239,13 @@ int build_tiles(fvs_handle* H, const Layout<T>& L, const std::vector<int>& tile_
   up = up && A.upload(dfgeo, fgeo) && A.upload(dgcell, gcell);
   tv.fgeo = dfgeo;
   tv.gcell = dgcell;
+  // one norm partial per tile block (tiles hold at least tile_cells / 2
+  // cells, so there can be more tiles than 256-cell blocks)
+  if (P.ntiles > H->nblk) {
+    void* q = nullptr;
+    if (!A.alloc(q, 32 * (size_t)P.ntiles)) return H->fail(FVS_ERR_NOMEM, "norm partials of the tile plan");
+    H->d.partials = static_cast<double*>(q);
+  }
   tv.nbuf = H->o.rk_nstages % 2 == 0 ? 2 : 3;
   tv.Pbuf[0] = H->d.Pv;
   for (int k = 1; k < tv.nbuf && up; k++) up = A.alloc(tv.Pbuf[k], sizeof(T) * 4 * (size_t)L.nc);
@@ -258,7 +266,7 @@ int build_device(fvs_handle* H) {
   if (fuse) {
     // tiles of compact patches (recursive coordinate bisection), reverse
     // Cuthill-McKee order within each tile
-    const std::vector<int> order = rcb_tile_order(H->hm, rcm_order(H->hm), TILE_CELLS, tile_start);
+    const std::vector<int> order = rcb_tile_order(H->hm, rcm_order(H->hm), tile_cells_setting(), tile_start);
     rc = append_case(L, H->hm, fold_w, 0, err, &order);
   } else {
     rc = append_case(L, H->hm, fold_w, 0, err);
@@ -941,13 +949,14 @@ int fvs_tile_plan_info(const fvs_mesh* mesh, const fvs_options* opt, int32_t* in
   rc = build_host_mesh(mesh, &o, hm, err);
   if (rc) { g_create_error = err; return rc; }
   std::vector<int> tile_start;
-  const std::vector<int> order = rcb_tile_order(hm, rcm_order(hm), TILE_CELLS, tile_start);
+  const std::vector<int> order = rcb_tile_order(hm, rcm_order(hm), tile_cells_setting(), tile_start);
   Layout<float> L;
   rc = append_case(L, hm, true, 0, err, &order);
   if (rc) { g_create_error = err; return rc; }
   TilePlan P;
   rc = build_tile_plan(tile_start, L.ecell, L.cf, L.st_ptr, L.st_cell, P, err);
   if (rc) { g_create_error = err; return rc; }
+  P.tile_cells = tile_cells_setting();
   const std::string bad = check_tile_plan(P, L.nc, L.ne, L.ecell, L.cf, L.st_ptr);
   info[0] = P.ntiles; info[1] = P.lmax; info[2] = P.gmax; info[3] = P.fmax; info[4] = bad.empty() ? 1 : 0;
   info[5] = (int32_t)P.halo.size();

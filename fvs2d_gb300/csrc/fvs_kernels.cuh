@@ -963,22 +963,26 @@ __device__ __forceinline__ void cons2prim(T g, const double* u, T* p) {
 
 // deterministic block sum of 4 doubles (shared-memory tree: one add per
 // element instead of five shuffle-adds per lane); thread 0 gets the sums
-__device__ __forceinline__ void block_sum4(const double* v, double* out) {
-  __shared__ double sh[4][256];
+// sh: 4 x 256 doubles of shared memory
+__device__ __forceinline__ void block_sum4_in(const double* v, double* out, double* sh) {
   const int t = threadIdx.x;
 #pragma unroll
-  for (int k = 0; k < 4; k++) sh[k][t] = v[k];
+  for (int k = 0; k < 4; k++) sh[256 * k + t] = v[k];
   __syncthreads();
   for (int w = blockDim.x >> 1; w > 0; w >>= 1) {
     if (t < w) {
 #pragma unroll
-      for (int k = 0; k < 4; k++) sh[k][t] += sh[k][t + w];
+      for (int k = 0; k < 4; k++) sh[256 * k + t] += sh[256 * k + t + w];
     }
     __syncthreads();
   }
   if (t == 0)
 #pragma unroll
-    for (int k = 0; k < 4; k++) out[k] = sh[k][0];
+    for (int k = 0; k < 4; k++) out[k] = sh[256 * k];
+}
+__device__ __forceinline__ void block_sum4(const double* v, double* out) {
+  __shared__ double sh[4 * 256];
+  block_sum4_in(v, out, sh);
 }
 
 #if FVS_MIXED
@@ -1191,13 +1195,13 @@ __device__ __forceinline__ void update_item(const DevView& d, const StageParams&
 
 // RMS of |U - U0| per component from the block partials, by one block of
 // 256 threads in a fixed order (deterministic); advances the step counter
-__device__ __forceinline__ void norm_final_block(const DevView& d) {
+__device__ __forceinline__ void norm_final_block(const DevView& d, double* sh) {
   double s[4] = {0.0, 0.0, 0.0, 0.0};
   for (int i = threadIdx.x; i < d.nblk_red; i += blockDim.x)
 #pragma unroll
     for (int k = 0; k < 4; k++) s[k] += __ldcg(d.partials + 4 * i + k);
   double out[4];
-  block_sum4(s, out);
+  block_sum4_in(s, out, sh);
   if (threadIdx.x == 0) {
     const int istep = d.stepctl[0] + 1;
     double* o = d.norms + 4 * (size_t)((istep - 1) % d.norm_cap);
@@ -1207,15 +1211,13 @@ __device__ __forceinline__ void norm_final_block(const DevView& d) {
   }
 }
 
-// One RK stage over all cells.  At the last stage every block writes its
-// partial norms; the block that finishes last (a counter in stepctl[1])
-// reduces them, so no separate norm launch is needed.
 // the block's sum of d2 into partials[blockIdx.x]; the block that finishes
-// last (d.nblk_red == gridDim.x) reduces all partials into the step's norms
-__device__ __forceinline__ void stage_norms(const DevView& d, const double* d2) {
+// last (d.nblk_red == gridDim.x) reduces all partials into the step's norms;
+// sh: 4 x 256 doubles of shared memory
+__device__ __forceinline__ void stage_norms(const DevView& d, const double* d2, double* sh) {
   __shared__ int s_last;
   double out[4];
-  block_sum4(d2, out);
+  block_sum4_in(d2, out, sh);
   if (threadIdx.x == 0) {
 #pragma unroll
     for (int k = 0; k < 4; k++) d.partials[4 * blockIdx.x + k] = out[k];
@@ -1225,11 +1227,14 @@ __device__ __forceinline__ void stage_norms(const DevView& d, const double* d2) 
   __syncthreads();
   if (s_last) {
     __threadfence();
-    norm_final_block(d);
+    norm_final_block(d, sh);
     if (threadIdx.x == 0) d.stepctl[1] = 0;
   }
 }
 
+// One RK stage over all cells.  At the last stage every block writes its
+// partial norms; the block that finishes last (a counter in stepctl[1])
+// reduces them, so no separate norm launch is needed.
 template <int MODE>
 __global__ void __launch_bounds__(256) k_update(const DevView d, const StageParams sp) {
   pdl_wait();
@@ -1237,7 +1242,8 @@ __global__ void __launch_bounds__(256) k_update(const DevView d, const StagePara
   const int ic = blockIdx.x * blockDim.x + threadIdx.x;
   double d2[4] = {0.0, 0.0, 0.0, 0.0};
   if (ic < d.nc) update_item<MODE, false>(d, sp, ic, d2);
-  if (sp.last) stage_norms(d, d2);
+  __shared__ double sh[4 * 256];
+  if (sp.last) stage_norms(d, d2, sh);
 }
 
 #if FVS_MIXED || FVS_DF
@@ -1248,7 +1254,8 @@ __global__ void __launch_bounds__(256) k_update(const DevView d, const StagePara
 // (lmax x 4), gradients and limiter values of the tile and halo1 (gmax x 9),
 // and the flux * area and ws * area of the tile's faces (fmax x 5).
 static size_t tile_smem_bytes(int lmax, int gmax, int fmax) {
-  return sizeof(T) * (4 * (size_t)lmax + 9 * (size_t)gmax + 5 * (size_t)fmax);
+  const size_t b = sizeof(T) * (4 * (size_t)lmax + 9 * (size_t)gmax + 5 * (size_t)fmax);
+  return b > 4 * 256 * sizeof(double) ? b : 4 * 256 * sizeof(double);
 }
 
 // One RK stage of one tile in four phases separated by block barriers:
@@ -1266,7 +1273,7 @@ static size_t tile_smem_bytes(int lmax, int gmax, int fmax) {
 // instructions, so both cells receive the same flux.  Results are
 // bit-identical to the separate gradient, flux and update kernels.
 template <int MODE, int REC, int LIM>
-__global__ void __launch_bounds__(256) k_tile_stage(const DevView d, const TileView tv, const StageParams sp, int kin,
+__global__ void __launch_bounds__(256, FVS_MIXED ? 5 : 2) k_tile_stage(const DevView d, const TileView tv, const StageParams sp, int kin,
                                                    int kout) {
   pdl_wait();
   pdl_trigger();
@@ -1377,7 +1384,9 @@ __global__ void __launch_bounds__(256) k_tile_stage(const DevView d, const TileV
     apply_stage_d<MODE, false>(d, sp, gid, res, ws, Pout, d2);
 #endif
   }
-  if (sp.last) stage_norms(d, d2);
+  // the norm reduction reuses the primitives' shared memory, unused in
+  // phase 4 (at least 4 x 256 doubles: tile_smem_bytes)
+  if (sp.last) stage_norms(d, d2, reinterpret_cast<double*>(tile_shm));
 }
 
 template <int MODE, int REC, int LIM>
@@ -1412,7 +1421,7 @@ static size_t tile_smem(int lmax, int gmax, int fmax) {
   if (cudaGetDevice(&dev) != cudaSuccess ||
       cudaDeviceGetAttribute(&cap, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess)
     return 0;
-  if (bytes + 4 * 256 * sizeof(double) + 64 > (size_t)cap) return 0;
+  if (bytes + 64 > (size_t)cap) return 0;
   const int b = (int)bytes;
   bool ok = true;
 #define FVS_TILE_ATTR(M)                                                                                           \

@@ -26,6 +26,7 @@
 #pragma once
 
 #include <algorithm>
+#include <cstdlib>
 #include <cstdint>
 #include <numeric>
 #include <string>
@@ -36,6 +37,13 @@
 namespace fvs {
 
 constexpr int TILE_CELLS = 512;
+
+// tile size: TILE_CELLS, or FVS2D_TILE_CELLS (64..4096) from the environment
+inline int tile_cells_setting() {
+  const char* e = std::getenv("FVS2D_TILE_CELLS");
+  const int v = e ? std::atoi(e) : 0;
+  return (v >= 64 && v <= 4096) ? v : TILE_CELLS;
+}
 
 // reference cell -> local device index: tiles of at most tile_cells cells by
 // recursive coordinate bisection; within a tile, cells in the order of
@@ -86,7 +94,7 @@ inline std::vector<int> rcb_tile_order(const HostMesh& h, const std::vector<int>
 }
 
 struct TilePlan {
-  int ntiles = 0;
+  int ntiles = 0, tile_cells = TILE_CELLS;
   int lmax = 0, gmax = 0, fmax = 0;  // largest local cell, gradient cell and face counts
   std::vector<int> c0;               // [ntiles + 1]
   std::vector<int> h0;               // [ntiles + 1] offsets into halo
@@ -216,7 +224,7 @@ inline std::string check_tile_plan(const TilePlan& P, int nc, int ne, const std:
   for (int t = 0; t < P.ntiles; t++) {
     const int b = P.c0[t], n = P.c0[t + 1] - b;
     const int nh = P.h0[t + 1] - P.h0[t], nl = n + nh, ng = n + P.nh1[t], nf = P.f0[t + 1] - P.f0[t];
-    if (n <= 0 || n > TILE_CELLS) return bad("tile size outside 1..TILE_CELLS", t);
+    if (n <= 0 || n > P.tile_cells) return bad("tile size outside 1..tile_cells", t);
     if (P.nh1[t] < 0 || P.nh1[t] > nh) return bad("halo1 count", t);
     if (nl > P.lmax || ng > P.gmax || nf > P.fmax || nl > 0xFFFE) return bad("counts above the plan maxima", t);
     for (int i = P.h0[t]; i < P.h0[t + 1]; i++)
