@@ -177,12 +177,16 @@ struct fvs_handle {
 
 namespace {
 
-// The fused RK stage runs for mixed and double-float handles unless the
-// environment variable FVS2D_TILE_STAGE is "0" at fvs_create.
+// The fused RK stage runs for mixed and double-float handles when the
+// environment variable FVS2D_TILE_STAGE is "1" at fvs_create.  It is off by
+// default: on GB300 the three separate kernels are faster (1,048,576-cell
+// vortex, per SSP-RK3 step: mixed 0.262 against 0.310 ms, double-float 0.656
+// against 1.014 ms), because each tile block runs its four phases one after
+// the other between barriers, latency-bound at 24-40 resident warps per SM.
 bool want_fused(const fvs_handle* H) {
   if (H->o.precision != FVS_PREC_MIXED && H->o.precision != FVS_PREC_FP64_DF) return false;
   const char* e = std::getenv("FVS2D_TILE_STAGE");
-  return !(e && e[0] == '0' && e[1] == 0);
+  return e && e[0] == '1' && e[1] == 0;
 }
 
 // Tile plan of a fused handle from its device-order layout: plan arrays,
