@@ -199,14 +199,30 @@ def traffic_from_profile(kernel: str):
 
 def pipe_note(kernel: str):
     """The compute pipe that binds a kernel, from the committed ncu summary
-    (the fourth column of profiles/ncu_traffic.txt, when present)."""
+    (the fifth column of profiles/ncu_traffic.txt, when present)."""
     path = os.path.join(ROOT, "profiles", "ncu_traffic.txt")
     if not os.path.exists(path):
         return None
     for line in open(path):
-        t = line.split(None, 3)
+        t = line.split(None, 4)
+        if len(t) >= 5 and not line.startswith("#") and t[0] == kernel:
+            return t[4].strip()
+    return None
+
+
+def fp64_pipe_frac(kernel: str):
+    """sm__pipe_fp64_cycles_active of a kernel as a fraction of peak, from the
+    committed ncu summary (the fourth column of profiles/ncu_traffic.txt)."""
+    path = os.path.join(ROOT, "profiles", "ncu_traffic.txt")
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        t = line.split()
         if len(t) >= 4 and not line.startswith("#") and t[0] == kernel:
-            return t[3].strip()
+            try:
+                return round(float(t[3]) / 100.0, 4)
+            except ValueError:
+                return None
     return None
 
 
@@ -288,6 +304,7 @@ def run_ours(args) -> dict:
                 "kernel_share": {k: round(v / sum(total.values()), 4) for k, v in total.items()},
                 "step_bytes_model": "252 B per cell-stage (ideal fused LSQ-fn FP64 stage)",
                 "compute_bound": pipe_note(f"{dom}:{args.precision}"),
+                "fp64_pipe_frac": fp64_pipe_frac(f"{dom}:{args.precision}"),
                 "step_frac_of_hbm": round(value / ws * 252 / (peak * 1e9), 4)}
 
     # end to end through the C-ABI with pinned host buffers
