@@ -16,9 +16,10 @@ all cells; the metric is cell-stage updates/s = ncells * 3 * steps / time.
   roofline  dominant kernel: algorithmic bytes per launch / mean launch time
   cpu_baseline  the CPU oracle (a restatement of the Fortran reference) on
             the host cores, on a bounded sample of the same workload
-  time_to_drop  wall time to a 1e-10 residual drop on the 261,120-cell
-            NACA0012 O-grid: plain FP64 solver against the batched precision
-            ladder (rank 0 only)
+  time_to_drop  wall time to a 1e-10 residual drop: the 261,120-cell
+            NACA0012 O-grid (plain FP64 solver against the batched precision
+            ladder) and an 8-case held-out airfoil sweep (plain FP64 against
+            batched and learned+batched); rank 0 only
 
 --impl reference times the reference's CPU algorithm (the oracle port: the
 Fortran reference cannot be built without a Fortran compiler and MPI) on all
@@ -356,16 +357,26 @@ def run_ours(args) -> dict:
 
 
 def time_to_drop() -> dict:
-    """The second half of the headline metric: wall time to a 1e-10 drop of
-    every RMS(dU) component on the 261,120-cell NACA0012 O-grid (M 0.8,
-    1.25 deg, steady SSP-RK(4,2), local dt at CFL 1.25), the plain FP64
-    solver against the batched precision ladder (mixed, then defect
-    correction, then an FP64 check), with its own clock record."""
+    """The second half of the headline metric, wall time to a 1e-10 drop of
+    every RMS(dU) component, each with its own clock record:
+      airfoil  the 261,120-cell NACA0012 O-grid (M 0.8, 1.25 deg, steady
+               SSP-RK(4,2), local dt at CFL 1.25): the plain FP64 solver
+               against the batched precision ladder (mixed, then defect
+               correction, then an FP64 check)
+      sweep    8 held-out airfoil cases of the reduced sweep distribution
+               (W 64-192, R 32-96, Mach 0.3-0.85, AoA -2..4 deg): plain FP64,
+               one solver per case, against the batched ladder from the free
+               stream and from the learned warm start (an MLP trained on the
+               GPU on 16 other cases' converged solutions)"""
     from fvs2d_gb300 import sweep_bench
+    out = {}
     clk = clock_sampler(0)
-    r = sweep_bench.run_airfoil()
-    r["clocks"] = clk.stop()
-    return r
+    out["airfoil"] = sweep_bench.run_airfoil()
+    out["airfoil"]["clocks"] = clk.stop()
+    clk = clock_sampler(0)
+    out["sweep"] = sweep_bench.run(n_train=16, n_test=8, race=False)
+    out["sweep"]["clocks"] = clk.stop()
+    return out
 
 
 def max_over_ranks(seconds: float, device: str) -> float:
@@ -464,7 +475,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=12.0)
     ap.add_argument("--no-time-to-drop", dest="time_to_drop", action="store_false",
-                    help="skip the time-to-1e-10-drop measurement on the NACA0012 O-grid (about 45 s)")
+                    help="skip the time-to-1e-10-drop measurements (NACA0012 O-grid and an 8-case sweep, "
+                         "about 90 s)")
     ap.add_argument("--workload", default="vortex", choices=["vortex", "sweep", "sweep-256", "airfoil",
                                                              "airfoil-limited", "vortex-period"],
                     help="vortex: the 1,048,576-cell throughput case (default); sweep: time to a 1e-10 drop on an "

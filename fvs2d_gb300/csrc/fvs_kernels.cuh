@@ -1026,7 +1026,13 @@ __device__ __forceinline__ void cell_residual_f(const DevView& d, int ic, bool w
 }
 
 // the RK stage of one cell from its residual res (and, at a steady first
-// stage, its wave-speed sum ws); the new primitives go to Pout
+// stage, its wave-speed sum ws); the new primitives go to Pout.
+// The FP64 state U stays the state at the start of the step until the last
+// stage writes the new one: each stage's state is U plus an FP32 increment
+// (the form above), so an intermediate stage needs only U and, carried in
+// the FP32 accumulator F, the accumulated residuals (SSP-RK(4,2), RK) or the
+// previous increment (SSP-RK3).  Per cell and SSP-RK3 step that is 192 bytes
+// of state traffic instead of 288 for writing U (and U0) at every stage.
 template <int MODE, bool COH>
 __device__ __forceinline__ void apply_stage_f(const DevView& d, const StageParams& sp, int ic, const float* res,
                                               float ws, float* Pout, double* d2) {
@@ -1044,14 +1050,12 @@ __device__ __forceinline__ void apply_stage_f(const DevView& d, const StageParam
   float* F = reinterpret_cast<float*>(d.F);
   double u0[4], u[4];
   float f[4], inc[4];
+  ldc4<COH>(d.U, ic, u0);  // the state at the start of the step
   if (sp.stage == 1) {
-    ldc4<COH>(d.U, ic, u0);
-    st4(d.U0, ic, u0);
 #pragma unroll
     for (int v = 0; v < 4; v++) f[v] = 0.f;
   } else {
-    ldc4<COH>(d.U0, ic, u0);
-    if (MODE != MODE_SSP3) ldc4<COH>(F, ic, f);
+    ldc4<COH>(F, ic, f);
   }
   const float coef = float(sp.coef);
   if (MODE == MODE_SSP42) {
@@ -1081,17 +1085,17 @@ __device__ __forceinline__ void apply_stage_f(const DevView& d, const StageParam
         u[v] = u0[v] + f2d_bits(inc[v]);
       }
     } else {
-      double cur[4];
-      ldc4<COH>(d.U, ic, cur);
+      // f: the previous stage's increment, its state minus u0
       const float b = float(sp.b);
 #pragma unroll
       for (int v = 0; v < 4; v++) {
-        inc[v] = b * (d2f_bits(cur[v] - u0[v]) + h * res[v]);
+        inc[v] = b * (f[v] + h * res[v]);
         u[v] = u0[v] + f2d_bits(inc[v]);
       }
     }
+    if (!sp.last) st4(F, ic, inc);
   }
-  st4(d.U, ic, u);
+  if (sp.last) st4(d.U, ic, u);
   float p[4];
   cons2prim(TP(gm1), u, p);
   st4(Pout, ic, p);
