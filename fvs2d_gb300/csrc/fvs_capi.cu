@@ -147,6 +147,7 @@ struct fvs_handle {
   // fused RK stage (mixed and double-float): cells in tile order, one
   // launch per stage (k_tile_stage)
   bool fused = false;
+  int tile_mode = 0;  // 1: the whole stage per tile; 2: flux + update per tile
   TileView tv;
   // d with one norm partial per tile block, for the fused stage
   DevView tile_view() const {
@@ -183,10 +184,14 @@ namespace {
 // vortex, per SSP-RK3 step: mixed 0.262 against 0.310 ms, double-float 0.656
 // against 1.014 ms), because each tile block runs its four phases one after
 // the other between barriers, latency-bound at 24-40 resident warps per SM.
-bool want_fused(const fvs_handle* H) {
-  if (H->o.precision != FVS_PREC_MIXED && H->o.precision != FVS_PREC_FP64_DF) return false;
+// FVS2D_TILE_STAGE=2 selects the lighter fusion: the gradient kernel as
+// before, then face flux and update in one launch per tile
+// (k_tile_flux_update).  Returns the mode: 0 none, 1 full, 2 flux + update.
+int want_fused(const fvs_handle* H) {
+  if (H->o.precision != FVS_PREC_MIXED && H->o.precision != FVS_PREC_FP64_DF) return 0;
   const char* e = std::getenv("FVS2D_TILE_STAGE");
-  return e && e[0] == '1' && e[1] == 0;
+  if (!e || e[1] != 0) return 0;
+  return e[0] == '1' ? 1 : e[0] == '2' ? 2 : 0;
 }
 
 // Tile plan of a fused handle from its device-order layout: plan arrays,
@@ -264,7 +269,7 @@ int build_device(fvs_handle* H) {
   Layout<T> L;
   std::string err;
   const bool fold_w = H->o.precision != FVS_PREC_FP64_STRICT;
-  const bool fuse = want_fused(H);
+  const int fuse = want_fused(H);
   std::vector<int> tile_start;
   int rc;
   if (fuse) {
@@ -294,6 +299,7 @@ int build_device(fvs_handle* H) {
   if (fuse && H->ks->tile_stage) {
     rc = build_tiles<T>(H, L, tile_start, H->fused);
     if (rc) return rc;
+    H->tile_mode = H->fused ? fuse : 0;
   }
   return FVS_OK;
 }
@@ -325,9 +331,18 @@ void enqueue_step(fvs_handle* H) {
   const KernelSet& K = *H->ks;
   cudaStream_t s = H->stream;
   K.begin_step(H->d, s);
-  if (H->fused) {
+  if (H->tile_mode == 1) {
     const DevView dv = H->tile_view();
     for (size_t k = 0; k < H->stages.size(); k++) K.tile_stage(dv, H->tv, H->stages[k], (int)k, s);
+    return;
+  }
+  if (H->tile_mode == 2) {
+    for (size_t k = 0; k < H->stages.size(); k++) {
+      DevView dk = H->tile_view();
+      dk.Pv = H->tv.Pbuf[k % H->tv.nbuf];
+      K.gradient(dk, s);
+      K.tile_fu_stage(dk, H->tv, H->stages[k], (int)k, s);
+    }
     return;
   }
   for (const StageParams& sp : H->stages) {
@@ -340,7 +355,8 @@ void enqueue_step(fvs_handle* H) {
 int count_launches(const fvs_handle* H) {
   // k_begin_step, then gradient (second order), flux and update per stage,
   // or one fused tile stage; the last stage also reduces the norms
-  int per_stage = H->fused ? 1 : (H->d.first_order ? 0 : 1) + 2;
+  const int grad = H->d.first_order ? 0 : 1;
+  int per_stage = H->tile_mode == 1 ? 1 : H->tile_mode == 2 ? grad + 1 : grad + 2;
   return 1 + per_stage * (int)H->stages.size();
 }
 
@@ -897,11 +913,20 @@ int fvs_profile_step(fvs_handle* h, int32_t cap, int32_t* n, char* names, float*
   };
   mark("start");
   K.begin_step(h->d, s);
-  if (h->fused) {
+  if (h->tile_mode == 1) {
     const DevView dv = h->tile_view();
     for (size_t k = 0; k < h->stages.size(); k++) {
       K.tile_stage(dv, h->tv, h->stages[k], (int)k, s);
       mark("tile_stage");
+    }
+  } else if (h->tile_mode == 2) {
+    for (size_t k = 0; k < h->stages.size(); k++) {
+      DevView dk = h->tile_view();
+      dk.Pv = h->tv.Pbuf[k % h->tv.nbuf];
+      K.gradient(dk, s);
+      if (!dk.first_order) mark("gradient");
+      K.tile_fu_stage(dk, h->tv, h->stages[k], (int)k, s);
+      mark("tile_flux_update");
     }
   } else {
     for (const StageParams& sp : h->stages) {

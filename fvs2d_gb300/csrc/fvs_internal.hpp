@@ -250,6 +250,9 @@ struct KernelSet {
   cudaError_t (*tile_stage)(const DevView&, const TileView&, const StageParams&, int k, cudaStream_t);
   // shared memory of one tile block for the plan's largest tile (bytes)
   size_t (*tile_smem)(int lmax, int gmax, int fmax);
+  // face flux + RK update of stage k over the tiles (gradients from the
+  // separate gradient kernel); d.Pv is the stage's input buffer
+  cudaError_t (*tile_fu_stage)(const DevView&, const TileView&, const StageParams&, int k, cudaStream_t);
 };
 // Defect correction of a first-order steady batch (mixed build): per chunk
 // the FP64 residual R0 of the base state is evaluated once; the RK stages

@@ -11,7 +11,8 @@ const KernelSet& kernels_mixed() {
   static const KernelSet k = {"mixed", k_mixed::launch_begin_step, k_mixed::launch_cvar2pvar, k_mixed::launch_gradient,
                               k_mixed::launch_flux, k_mixed::launch_update, k_mixed::launch_residual_out, k_mixed::persistent_occupancy,
                               k_mixed::launch_persistent, k_mixed::launch_tiled_step,
-                              k_mixed::launch_tile_stage, k_mixed::tile_smem};
+                              k_mixed::launch_tile_stage, k_mixed::tile_smem,
+                              k_mixed::launch_tile_fu_stage};
   return k;
 }
 const DcKernels& dc_kernels() {

@@ -732,8 +732,10 @@ __device__ __forceinline__ void face_states(const DevView& d, int e, bool interi
   }
 }
 
+// flux * area and ws * area of edge slot e from the cell data in global
+// memory (the edge-flux kernel's loads and arithmetic)
 template <int REC, bool COH>
-__device__ __forceinline__ void flux_item(const DevView& d, int e, double time) {
+__device__ __forceinline__ void flux_compute(const DevView& d, int e, double time, T* flux, T& wsa) {
   constexpr bool SPEC = REC == REC_SPEC;
   const T* P = static_cast<const T*>(d.Pv);
   const T* GX = static_cast<const T*>(d.Gx);
@@ -767,7 +769,15 @@ __device__ __forceinline__ void flux_item(const DevView& d, int e, double time) 
     if (interior) dr = ld2(d.edR, e);
   }
   face_states<REC>(d, e, interior, time, n, dl, dr, pl, gxl, gyl, phiL, pr, gxr, gyr, phiR, pfL, pfR);
-  flux_finish(d, e, pfL, pfR, n, af);
+  flux_eval(d, pfL, pfR, n, af, flux, wsa);
+}
+
+template <int REC, bool COH>
+__device__ __forceinline__ void flux_item(const DevView& d, int e, double time) {
+  T flux[4], wsa;
+  flux_compute<REC, COH>(d, e, time, flux, wsa);
+  st4(static_cast<T*>(d.eflux), e, flux);
+  static_cast<T*>(d.ews)[e] = wsa;
 }
 
 // First-order flux of two edge slots per call (e1 < 0: e0 alone).  The
@@ -1417,6 +1427,95 @@ static cudaError_t launch_tile_stage(const DevView& d, const TileView& tv, const
   return launch_tile_mode<MODE_RK>(d, tv, sp, k, s);
 }
 
+// ---------------------------------------------------------------------------
+// face flux + update per tile (gradients from the separate gradient kernel)
+// ---------------------------------------------------------------------------
+// One block per tile: the fluxes of every face of the tile (the edge-flux
+// kernel's loads from global memory and its arithmetic) into shared memory,
+// then the tile's cells summed in their gather order and updated (the update
+// kernel's arithmetic).  The flux records never go through global memory, a
+// stage has two launches instead of three, and shared memory holds only the
+// fluxes, so occupancy stays that of the separate kernels.  The primitives
+// alternate between buffers (a block's new values must not reach a
+// neighbouring tile that still reads the old ones for a cut face).
+// Bit-identical to the separate flux and update kernels.
+static size_t tile_fu_smem_bytes(int fmax) {
+  const size_t b = 5 * sizeof(T) * (size_t)fmax;
+  return b > 4 * 256 * sizeof(double) ? b : 4 * 256 * sizeof(double);
+}
+
+template <int MODE, int REC>
+__global__ void __launch_bounds__(256) k_tile_flux_update(const DevView d, const TileView tv, const StageParams sp,
+                                                         int kout) {
+  pdl_wait();
+  pdl_trigger();
+  extern __shared__ __align__(16) unsigned char tile_shm[];
+  T* sF = reinterpret_cast<T*>(tile_shm);
+  const int t = blockIdx.x, tid = threadIdx.x, nthr = blockDim.x;
+  const int b = tv.c0[t], n = tv.c0[t + 1] - b;
+  T* Pout = static_cast<T*>(tv.Pbuf[kout]);
+  const double time = d.tctl[1] + sp.dts;
+  const int fb = tv.f0[t], nf = tv.f0[t + 1] - fb;
+  for (int f = tid; f < nf; f += nthr) {
+    T flux[4], wsa;
+    flux_compute<REC, false>(d, tv.face[fb + f], time, flux, wsa);
+#pragma unroll
+    for (int v = 0; v < 4; v++) sF[5 * f + v] = flux[v];
+    sF[5 * f + 4] = wsa;
+  }
+  __syncthreads();
+  double d2[4] = {0.0, 0.0, 0.0, 0.0};
+  const bool want_ws = sp.steady && sp.stage == 1;
+  for (int i = tid; i < n; i += nthr) {
+    const int gid = b + i;
+    const int2 q = tv.lcf[gid];
+    const int sl[4] = {(int)(int16_t)(q.x & 0xFFFF), (int)(int16_t)((unsigned)q.x >> 16),
+                       (int)(int16_t)(q.y & 0xFFFF), (int)(int16_t)((unsigned)q.y >> 16)};
+    auto get = [&](int idx, T* f, T& w) {
+#pragma unroll
+      for (int v = 0; v < 4; v++) f[v] = sF[5 * idx + v];
+      w = sF[5 * idx + 4];
+    };
+#if FVS_MIXED
+    float res[4], ws;
+    residual_from_faces_f(sl, -static_cast<const float*>(d.volT)[gid], want_ws, get, res, ws);
+    apply_stage_f<MODE, false>(d, sp, gid, res, ws, Pout, d2);
+#else
+    double res[4], ws;
+    const df64 rv = -static_cast<const df64*>(d.volT)[gid];
+    if (want_ws) residual_from_faces_df<true>(sl, rv, get, res, ws);
+    else residual_from_faces_df<false>(sl, rv, get, res, ws);
+    apply_stage_d<MODE, false>(d, sp, gid, res, ws, Pout, d2);
+#endif
+  }
+  if (sp.last) {
+    __syncthreads();  // the norm buffer reuses the flux records
+    stage_norms(d, d2, reinterpret_cast<double*>(tile_shm));
+  }
+}
+
+template <int MODE>
+static cudaError_t launch_tile_fu_mode(const DevView& d, const TileView& tv, const StageParams& sp, int k,
+                                       cudaStream_t s) {
+  const bool spec = d.khalf == 0.0 && d.omk == 1.0 && d.limiter == FVS_LIM_NONE;
+  const unsigned g = (unsigned)tv.ntiles;
+  const size_t sm = tile_fu_smem_bytes(tv.fmax);
+  const int ko = (k + 1) % tv.nbuf;
+  if (d.first_order) launch_k(k_tile_flux_update<MODE, REC_FIRST>, g, 256, sm, s, d, tv, sp, ko);
+  else if (spec) launch_k(k_tile_flux_update<MODE, REC_SPEC>, g, 256, sm, s, d, tv, sp, ko);
+  else launch_k(k_tile_flux_update<MODE, REC_GENERAL>, g, 256, sm, s, d, tv, sp, ko);
+  return cudaGetLastError();
+}
+
+// the tile flux+update of stage k; d.Pv must be the stage's input buffer
+// Pbuf[k % nbuf] (the gradient kernel, launched before it, reads the same)
+static cudaError_t launch_tile_fu_stage(const DevView& d, const TileView& tv, const StageParams& sp, int k,
+                                        cudaStream_t s) {
+  if (sp.mode == MODE_SSP42) return launch_tile_fu_mode<MODE_SSP42>(d, tv, sp, k, s);
+  if (sp.mode == MODE_SSP3) return launch_tile_fu_mode<MODE_SSP3>(d, tv, sp, k, s);
+  return launch_tile_fu_mode<MODE_RK>(d, tv, sp, k, s);
+}
+
 // opts every instantiation in to the shared memory of the plan's largest
 // tile; returns the bytes of one block (0: more than a block may have)
 static size_t tile_smem(int lmax, int gmax, int fmax) {
@@ -1441,6 +1540,18 @@ static size_t tile_smem(int lmax, int gmax, int fmax) {
   FVS_TILE_ATTR(MODE_SSP3);
   FVS_TILE_ATTR(MODE_RK);
 #undef FVS_TILE_ATTR
+  const int bf = (int)tile_fu_smem_bytes(fmax);
+#define FVS_TILE_FU_ATTR(M)                                                                                         \
+  ok = ok && cudaFuncSetAttribute(k_tile_flux_update<M, REC_FIRST>, cudaFuncAttributeMaxDynamicSharedMemorySize,   \
+                                  bf) == cudaSuccess;                                                              \
+  ok = ok && cudaFuncSetAttribute(k_tile_flux_update<M, REC_SPEC>, cudaFuncAttributeMaxDynamicSharedMemorySize,    \
+                                  bf) == cudaSuccess;                                                              \
+  ok = ok && cudaFuncSetAttribute(k_tile_flux_update<M, REC_GENERAL>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                                  bf) == cudaSuccess
+  FVS_TILE_FU_ATTR(MODE_SSP42);
+  FVS_TILE_FU_ATTR(MODE_SSP3);
+  FVS_TILE_FU_ATTR(MODE_RK);
+#undef FVS_TILE_FU_ATTR
   return ok ? bytes : 0;
 }
 #endif  // FVS_MIXED || FVS_DF

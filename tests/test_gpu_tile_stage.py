@@ -1,7 +1,8 @@
-"""The fused RK stage (k_tile_stage: one thread block per tile of cells,
-gradients and face fluxes kept in shared memory) against the separate
-gradient, flux and update kernels, for the mixed and double-float
-precisions, through the C-ABI.
+"""The fused RK stages against the separate gradient, flux and update
+kernels, for the mixed and double-float precisions, through the C-ABI:
+k_tile_stage (one thread block per tile of cells, gradients and face fluxes
+kept in shared memory) and k_tile_flux_update (after the gradient kernel,
+face fluxes in shared memory and the update, per tile).
 
 Both handles run the same per-cell arithmetic in the same summation order;
 only the cell numbering (tiles of compact patches against reverse
@@ -35,8 +36,8 @@ CASES = {
 }
 
 
-def run(mesh, opt, fused, monkeypatch, steps=6):
-    monkeypatch.setenv("FVS2D_TILE_STAGE", "1" if fused else "0")
+def run(mesh, opt, mode, monkeypatch, steps=6):
+    monkeypatch.setenv("FVS2D_TILE_STAGE", str(mode))
     with Solver(mesh, opt) as s:
         s.initialize_solution()
         launches = s.launches_per_step()
@@ -47,15 +48,22 @@ def run(mesh, opt, fused, monkeypatch, steps=6):
     return launches, norms, u, r, w
 
 
+@pytest.mark.parametrize("mode", [1, 2])
 @pytest.mark.parametrize("prec", [PREC_MIXED, PREC_FP64_DF])
 @pytest.mark.parametrize("name", sorted(CASES))
-def test_tile_stage_bit_identical_to_separate_kernels(name, prec, monkeypatch):
+def test_tile_stage_bit_identical_to_separate_kernels(name, prec, mode, monkeypatch):
+    """mode 1: the whole stage in one launch per tile (k_tile_stage); mode 2:
+    the gradient kernel, then face flux and update in one launch per tile
+    (k_tile_flux_update)."""
     mesh, opt = CASES[name]()
     opt = opt.replace(precision=prec)
-    lf, nf, uf, rf, wf = run(mesh, opt, True, monkeypatch)
-    ls, ns, us, rs, ws = run(mesh, opt, False, monkeypatch)
+    lf, nf, uf, rf, wf = run(mesh, opt, mode, monkeypatch)
+    ls, ns, us, rs, ws = run(mesh, opt, 0, monkeypatch)
     nst = opt.rk_nstages
-    assert lf == 1 + nst, lf  # k_begin_step + one fused launch per stage
+    grad = 0 if opt.reconst == 1 else 1
+    # k_begin_step + per stage one fused launch (mode 1) or gradient + one
+    # launch (mode 2)
+    assert lf == 1 + nst * (1 if mode == 1 else grad + 1), lf
     assert ls > lf
     assert np.array_equal(uf, us), float(np.abs(uf - us).max())
     assert np.array_equal(rf, rs) and np.array_equal(wf, ws)
