@@ -53,21 +53,25 @@ def case_options(c: Case, precision: int, first_order: bool = True) -> Options:
                    reconst=1 if first_order else 2, dt=0.01, precision=precision)
 
 
-def wall_distance(mesh: meshgen.Mesh, nw: int, xy: np.ndarray) -> np.ndarray:
-    """Distance from points to the wall polygon (nodes 1..nw of the O-grid)."""
+def wall_distance(mesh: meshgen.Mesh, nw: int, xy: np.ndarray, k: int = 8) -> np.ndarray:
+    """Distance from points to the wall polygon (nodes 1..nw of the O-grid):
+    the smallest distance to the segments on either side of the point's k
+    nearest wall nodes (a k-d tree query).  The nearest point of the polygon
+    lies on such a segment unless a segment longer than the distance between
+    k consecutive nodes passes closer; for the O-grid walls, whose nodes
+    follow the profile smoothly, this is the exact polygon distance."""
+    from scipy.spatial import cKDTree
     w = mesh.node_xy[:nw]
-    a = w
-    b = np.roll(w, -1, axis=0)
-    best = np.full(xy.shape[0], np.inf)
-    for i in range(0, nw, 64):
-        aa, bb = a[i:i + 64], b[i:i + 64]
-        ab = bb - aa
-        t = ((xy[:, None, :] - aa[None]) * ab[None]).sum(-1) / np.maximum((ab * ab).sum(-1), 1e-300)[None]
-        t = np.clip(t, 0.0, 1.0)
-        p = aa[None] + t[..., None] * ab[None]
-        dd = np.sqrt(((xy[:, None, :] - p) ** 2).sum(-1)).min(1)
-        best = np.minimum(best, dd)
-    return best
+    k = min(k, nw)
+    _, idx = cKDTree(w).query(xy, k=k)
+    idx = idx.reshape(xy.shape[0], k)
+    seg = np.concatenate([idx, (idx - 1) % nw], axis=1)  # segment s runs from node s to node s+1
+    a = w[seg]
+    ab = w[(seg + 1) % nw] - a
+    t = ((xy[:, None, :] - a) * ab).sum(-1) / np.maximum((ab * ab).sum(-1), 1e-300)
+    t = np.clip(t, 0.0, 1.0)
+    p = a + t[..., None] * ab
+    return np.sqrt(((xy[:, None, :] - p) ** 2).sum(-1)).min(1)
 
 
 def free_stream_state(c: Case, ncells: int, gamma: float = 1.4) -> np.ndarray:

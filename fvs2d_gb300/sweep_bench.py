@@ -22,12 +22,13 @@ metric).  Runs entirely on the GPU through the C-ABI; prints one JSON object.
 from __future__ import annotations
 
 import json
+import sys
 import time
 
 import numpy as np
 
 from . import PREC_FP64, PREC_MIXED, sweep
-from .warmstart import WarmStart, build_dataset, reference_levels, solve_ladder, solve_ladder_raced
+from .warmstart import WarmStart, build_dataset, features, reference_levels, solve_ladder, solve_ladder_raced
 
 
 def run(n_train=96, n_test=24, wall=(64, 192), radial=(32, 96), max_steps=400000, epochs=30, seed_train=5,
@@ -108,7 +109,7 @@ def run(n_train=96, n_test=24, wall=(64, 192), radial=(32, 96), max_steps=400000
     return out
 
 
-def run_scaled(n_train=256, n_test=256, n_plain=32, curve=(32, 64, 128, 256), wall=(64, 512), radial=(32, 256),
+def run_scaled(n_train=256, n_test=256, n_plain=16, curve=(32, 64, 128, 256), wall=(64, 512), radial=(32, 256),
                max_steps=400000, epochs=30, seed_train=5, seed_test=6, drop=1e-10, switch=1e-5):
     """The sweep at the stated scale: n_test held-out cases of the full
     distribution (W 64-512, R 32-256: ~21M cells for 256 cases) solved by the
@@ -124,18 +125,30 @@ def run_scaled(n_train=256, n_test=256, n_plain=32, curve=(32, 64, 128, 256), wa
            "scheme": "steady SSP-RK(4,2), local dt CFL 1.25, first-order Roe, slip wall + free stream",
            "target": f"RMS(dU_k) <= {drop:g} x first-step RMS(dU_k) of a free-stream start, k = 1..4"}
     opts = lambda cs: [sweep.case_options(c, PREC_MIXED) for c in cs]  # noqa: E731
+    t_start = time.perf_counter()
+
+    def progress(phase, **kw):
+        # one line per finished phase on stderr (the result is one JSON line on stdout)
+        print(json.dumps({"phase": phase, "elapsed_s": round(time.perf_counter() - t_start, 1), **kw}),
+              file=sys.stderr, flush=True)
+
     # ---- training solutions
     train = sweep.draw_cases(n_train, seed_train, wall, radial)
     tm = [c.mesh() for c in train]
+    feats_tr = [features(c, m) for c, m in zip(train, tm)]
+    progress("training meshes and features")
     lv_tr = reference_levels(train, tm)
     st_tr, t1, t2, t_tr, _ = solve_ladder(tm, opts(train), lv_tr, switch, drop, max_steps)
     out["training_solve"] = {"cells": int(sum(m.ncells for m in tm)), "seconds": round(t_tr, 2),
                              "steps_total": int((t1 + t2).sum())}
+    progress("training solve", **out["training_solve"])
     # ---- held-out sweep from the free stream
     test = sweep.draw_cases(n_test, seed_test, wall, radial)
     meshes = [c.mesh() for c in test]
+    feats_te = [features(c, m) for c, m in zip(test, meshes)]
     levels = reference_levels(test, meshes)
     st_b, b1, b2, t_b, ph_b = solve_ladder(meshes, opts(test), levels, switch, drop, max_steps)
+    progress("held-out batched ladder", seconds=round(t_b, 2), steps_total=int((b1 + b2).sum()))
     fs = [sweep.free_stream_state(c, m.ncells) for c, m in zip(test, meshes)]
 
     def rel_err(a, b):
@@ -149,21 +162,23 @@ def run_scaled(n_train=256, n_test=256, n_plain=32, curve=(32, 64, 128, 256), wa
     for m in curve:
         if m > n_train:
             continue
-        X, Y = build_dataset(train[:m], st_tr[:m])
+        X, Y = build_dataset(train[:m], st_tr[:m], feats=feats_tr[:m])
         t0 = time.perf_counter()
         ws = WarmStart(width=256, depth=4, seed=1)
         losses = ws.fit(X, Y, epochs=epochs, batch=4096, lr=1e-3, seed=2)
         t_fit = time.perf_counter() - t0
-        starts = [ws.predict_state(c, mm) for c, mm in zip(test, meshes)]
+        starts = [ws.predict_state(c, mm, f) for c, mm, f in zip(test, meshes, feats_te)]
         e_inf, e_l2 = rel_err(starts, st_b)
         rows.append({"train_solutions": m, "samples": int(X.shape[0]), "train_seconds": round(t_fit, 2),
                      "loss_first_last": [float(losses[0]), float(losses[-1])],
                      "surrogate_l2_median": float(np.median(e_l2)), "surrogate_linf_median": float(np.median(e_inf))})
+        progress("learning curve", **rows[-1])
     out["learning_curve"] = {"rows": rows, "free_stream_l2_median": float(np.median(fs_l2)),
                              "free_stream_linf_median": float(np.median(fs_inf))}
     # ---- held-out sweep from the learned start (largest network)
-    starts = [ws.predict_state(c, mm) for c, mm in zip(test, meshes)]
+    starts = [ws.predict_state(c, mm, f) for c, mm, f in zip(test, meshes, feats_te)]
     st_l, l1, l2, t_l, ph_l = solve_ladder(meshes, opts(test), levels, switch, drop, max_steps, starts=starts)
+    progress("held-out learned batched ladder", seconds=round(t_l, 2), steps_total=int((l1 + l2).sum()))
     l_inf, _ = rel_err(st_l, st_b)
     steps_b, steps_l = b1 + b2, l1 + l2
     out["all_cases"] = {
@@ -186,6 +201,7 @@ def run_scaled(n_train=256, n_test=256, n_plain=32, curve=(32, 64, 128, 256), wa
     sb, s1, s2, t_sb, _ = solve_ladder(meshes[sub], opts(test[sub]), levels[sub], switch, drop, max_steps)
     sl, u1, u2, t_sl, _ = solve_ladder(meshes[sub], opts(test[sub]), levels[sub], switch, drop, max_steps,
                                        starts=starts[sub])
+    progress("plain subset", seconds=round(t_p, 2), batched=round(t_sb, 2), learned=round(t_sl, 2))
     b_inf, _ = rel_err(sb, plain_states)
     lp_inf, _ = rel_err(sl, plain_states)
     out["plain_subset"] = {

@@ -132,8 +132,10 @@ class WarmStart:
         self.scale = np.maximum(Y.std(0), 1e-6).astype(np.float32)
         return self.net.train(X, Y / self.scale, batch=batch, epochs=epochs, lr=lr, seed=seed)
 
-    def predict_state(self, case: sweep.Case, mesh) -> np.ndarray:
-        f = features(case, mesh)
+    def predict_state(self, case: sweep.Case, mesh, feats: np.ndarray | None = None) -> np.ndarray:
+        """The predicted conservative state of a case (feats: its features,
+        when already computed)."""
+        f = features(case, mesh) if feats is None else feats
         dU = self.net.predict(f) * self.scale
         u = sweep.free_stream_state(case, f.shape[0]) + dU.astype(np.float64)
         # keep the state physical (positive density and pressure)
@@ -143,12 +145,14 @@ class WarmStart:
         return u
 
 
-def build_dataset(cases, states, max_cells_per_case=20000, seed=0):
+def build_dataset(cases, states, max_cells_per_case=20000, seed=0, feats=None):
+    """Training samples: per case at most max_cells_per_case cells (seeded
+    draw) of (features, converged state minus free stream); feats: the
+    cases' features when already computed."""
     rng = np.random.default_rng(seed)
     X, Y = [], []
-    for c, u in zip(cases, states):
-        mesh = c.mesh()
-        f = features(c, mesh)
+    for k, (c, u) in enumerate(zip(cases, states)):
+        f = features(c, c.mesh()) if feats is None else feats[k]
         t = targets(c, u)
         if f.shape[0] > max_cells_per_case:
             sel = rng.choice(f.shape[0], max_cells_per_case, replace=False)
