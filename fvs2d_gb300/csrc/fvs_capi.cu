@@ -147,8 +147,10 @@ struct fvs_handle {
   // fused RK stage (mixed and double-float): cells in tile order, one
   // launch per stage (k_tile_stage)
   bool fused = false;
-  int tile_mode = 0;  // 1: the whole stage per tile; 2: flux + update per tile
+  int tile_mode = 0;  // 1: the whole stage per tile; 2: flux + update per tile; 3: bulk-copy whole stage
   TileView tv;
+  TileDmaView dv;
+  bool gb_stale = true;  // the gather buffer does not hold the current primitives
   // d with one norm partial per tile block, for the fused stage
   DevView tile_view() const {
     DevView v = d;
@@ -187,10 +189,13 @@ namespace {
 // FVS2D_TILE_STAGE=2 selects the lighter fusion: the gradient kernel as
 // before, then face flux and update in one launch per tile
 // (k_tile_flux_update).  Returns the mode: 0 none, 1 full, 2 flux + update.
+// FVS2D_TILE_STAGE=3 selects the bulk-copy form (k_tile_dma; mixed handles
+// with LSQ gradients).
 int want_fused(const fvs_handle* H) {
   if (H->o.precision != FVS_PREC_MIXED && H->o.precision != FVS_PREC_FP64_DF) return 0;
   const char* e = std::getenv("FVS2D_TILE_STAGE");
   if (!e || e[1] != 0) return 0;
+  if (e[0] == '3') return (H->o.precision == FVS_PREC_MIXED && H->o.grad_method == FVS_GRAD_LSQ) ? 3 : 0;
   return e[0] == '1' ? 1 : e[0] == '2' ? 2 : 0;
 }
 
@@ -200,9 +205,8 @@ int want_fused(const fvs_handle* H) {
 // tile block's shared memory.  Returns false (handle stays unfused) when a
 // tile block would need more shared memory than a block may have.
 template <typename T>
-int build_tiles(fvs_handle* H, const Layout<T>& L, const std::vector<int>& tile_start, bool& ok) {
+int build_tiles(fvs_handle* H, const Layout<T>& L, const std::vector<int>& tile_start, bool& ok, TilePlan& P) {
   ok = false;
-  TilePlan P;
   std::string err;
   int rc = build_tile_plan(tile_start, L.ecell, L.cf, L.st_ptr, L.st_cell, P, err);
   if (rc) return H->fail(rc, err);
@@ -263,6 +267,53 @@ int build_tiles(fvs_handle* H, const Layout<T>& L, const std::vector<int>& tile_
   return FVS_OK;
 }
 
+// The bulk-copy plan of a fused handle (mode 3): segments, coefficients in
+// tile order, gather buffers, the error word and the shared-memory layout;
+// every copy's alignment and extent checked.  ok = false leaves the handle
+// on the separate kernels (a block would need too much shared memory).
+template <typename T>
+int build_tile_dma_view(fvs_handle* H, const Layout<T>& L, const TilePlan& P, bool& ok) {
+  ok = false;
+  std::string err;
+  TileDma D;
+  build_tile_dma(P, L.st_ptr, L.nc, D);
+  err = check_tile_dma(P, D, (int)sizeof(T), L.nc, L.st_cell.size());
+  if (!err.empty()) return H->fail(FVS_ERR_MESH, "bulk-copy tile plan: " + err);
+  std::vector<T> coef(2 * D.coef_src.size(), T(0));
+  for (size_t k = 0; k < D.coef_src.size(); k++)
+    if (D.coef_src[k] >= 0) {
+      coef[2 * k] = L.st_coef[2 * (size_t)D.coef_src[k]];
+      coef[2 * k + 1] = L.st_coef[2 * (size_t)D.coef_src[k] + 1];
+    }
+  TileDmaView& dv = H->dv;
+  dv.smax = D.smax; dv.pmax = D.pmax; dv.rmax = D.rmax; dv.qmax = D.qmax;
+  const DmaSmem m = dma_smem((int)sizeof(T), P.lmax, P.gmax, P.fmax, D.smax, D.pmax, D.rmax, D.qmax);
+  dv.o_P = (unsigned)m.P; dv.o_Fg = (unsigned)m.Fg; dv.o_C = (unsigned)m.C; dv.o_L = (unsigned)m.L;
+  dv.o_S = (unsigned)m.S; dv.o_R = (unsigned)m.Rr; dv.o_Q = (unsigned)m.Q; dv.o_Gx = (unsigned)m.Gx;
+  dv.o_Gy = (unsigned)m.Gy; dv.o_Ph = (unsigned)m.Ph; dv.o_F = (unsigned)m.F;
+  dv.smem_bytes = m.total;
+  if (H->ks->tile_dma_smem(H->tv, dv) == 0) return FVS_OK;
+  DeviceArena& A = H->arena;
+  int *gb0, *sb0, *pb0, *rb0, *cb0, *dptr, *dpos;
+  uint16_t *lst, *lsp;
+  uint32_t* flr;
+  int2* lcf;
+  T* dcoef;
+  bool up = A.upload(gb0, D.gb0) && A.upload(sb0, D.sb0) && A.upload(pb0, D.pb0) && A.upload(rb0, D.rb0) &&
+            A.upload(cb0, D.cb0) && A.upload(lst, D.lst) && A.upload(lsp, D.lsp) && A.upload(flr, D.flr) &&
+            A.upload(lcf, D.lcf) && A.upload(dcoef, coef) && A.upload(dptr, D.dptr) && A.upload(dpos, D.dpos);
+  dv.gb0 = gb0; dv.sb0 = sb0; dv.pb0 = pb0; dv.rb0 = rb0; dv.cb0 = cb0; dv.lst = lst; dv.lsp = lsp; dv.flr = flr;
+  dv.lcf = lcf; dv.coef = dcoef; dv.dptr = dptr; dv.dpos = dpos;
+  const size_t gbytes = sizeof(T) * 4 * (size_t)D.gb0.back();
+  for (int k = 0; k < H->tv.nbuf && up; k++) up = A.alloc(dv.GB[k], gbytes);
+  void* e = nullptr;
+  up = up && A.alloc(e, 16);
+  dv.err = static_cast<int*>(e);
+  if (!up) return H->fail(FVS_ERR_NOMEM, "device allocation or upload of the bulk-copy plan failed");
+  ok = true;
+  return FVS_OK;
+}
+
 // Builds every device array of the handle from the host mesh.
 template <typename T>
 int build_device(fvs_handle* H) {
@@ -297,9 +348,16 @@ int build_device(fvs_handle* H) {
   if (cudaMemcpy(d.phi, phi0.data(), sizeof(T) * L.nc, cudaMemcpyHostToDevice) != cudaSuccess)
     return H->fail(FVS_ERR_CUDA, "phi upload failed");
   if (fuse && H->ks->tile_stage) {
-    rc = build_tiles<T>(H, L, tile_start, H->fused);
+    TilePlan P;
+    rc = build_tiles<T>(H, L, tile_start, H->fused, P);
     if (rc) return rc;
     H->tile_mode = H->fused ? fuse : 0;
+    if (H->tile_mode == 3) {
+      bool ok = false;
+      rc = build_tile_dma_view<T>(H, L, P, ok);
+      if (rc) return rc;
+      if (!ok) H->tile_mode = 0;
+    }
   }
   return FVS_OK;
 }
@@ -336,6 +394,11 @@ void enqueue_step(fvs_handle* H) {
     for (size_t k = 0; k < H->stages.size(); k++) K.tile_stage(dv, H->tv, H->stages[k], (int)k, s);
     return;
   }
+  if (H->tile_mode == 3) {
+    const DevView dv = H->tile_view();
+    for (size_t k = 0; k < H->stages.size(); k++) K.tile_dma_stage(dv, H->tv, H->dv, H->stages[k], (int)k, s);
+    return;
+  }
   if (H->tile_mode == 2) {
     for (size_t k = 0; k < H->stages.size(); k++) {
       DevView dk = H->tile_view();
@@ -356,7 +419,7 @@ int count_launches(const fvs_handle* H) {
   // k_begin_step, then gradient (second order), flux and update per stage,
   // or one fused tile stage; the last stage also reduces the norms
   const int grad = H->d.first_order ? 0 : 1;
-  int per_stage = H->tile_mode == 1 ? 1 : H->tile_mode == 2 ? grad + 1 : grad + 2;
+  int per_stage = (H->tile_mode == 1 || H->tile_mode == 3) ? 1 : H->tile_mode == 2 ? grad + 1 : grad + 2;
   return 1 + per_stage * (int)H->stages.size();
 }
 
@@ -438,6 +501,7 @@ int state_in(fvs_handle* H, const double* cvar) {
   if (e != cudaSuccess) return H->cuda_fail(e, "state upload");
   k_scatter_in<<<(H->hm.nc + 255) / 256, 256, 0, H->stream>>>(H->d_stage, H->d_perm, H->d.U, H->hm.nc);
   H->ks->cvar2pvar(H->d, H->stream);
+  H->gb_stale = true;
   return check_launch(H, "state scatter");
 }
 
@@ -709,11 +773,35 @@ int fvs_get_gradient(fvs_handle* h, double* grad, double* phi) {
   return rc;
 }
 
+// bulk-copy handles: the gather buffer the first stage reads, from the
+// current primitives, when the state changed since the last step
+int refill_gather(fvs_handle* h) {
+  if (h->tile_mode != 3 || !h->gb_stale) return FVS_OK;
+  cudaError_t e = h->ks->tile_dma_fill(h->d, h->dv, 0, h->stream);
+  if (e != cudaSuccess) return h->cuda_fail(e, "gather buffer fill");
+  h->gb_stale = false;
+  return FVS_OK;
+}
+
+// bulk-copy handles: FVS_ERR_TIMEOUT when a block's wait for its copies ran
+// out (the word is cleared); call after the stream has been synchronised
+int dma_report(fvs_handle* h) {
+  if (h->tile_mode != 3) return FVS_OK;
+  int w = 0;
+  cudaError_t e = cudaMemcpy(&w, h->dv.err, sizeof w, cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return h->cuda_fail(e, "bulk-copy error word download");
+  if (!w) return FVS_OK;
+  cudaMemset(h->dv.err, 0, sizeof w);
+  h->gb_stale = true;
+  return h->fail(FVS_ERR_TIMEOUT, "a tile block's wait for its bulk copies ran out");
+}
+
 static int run_steps(fvs_handle* h, double t1, int nsteps, double* resnorm, float* ms) {
   NvtxRange nv("fvs time integration (graph replays)");
   int rc = ensure_dt(h, t1);
   if (rc) return rc;
   if ((rc = ensure_graph(h, 1))) return rc;
+  if ((rc = refill_gather(h))) return rc;
   // control words: t1, steps done = 0
   h->h_small[0] = t1;
   reinterpret_cast<int*>(h->h_small + 1)[0] = 0;  // steps done
@@ -746,6 +834,7 @@ static int run_steps(fvs_handle* h, double t1, int nsteps, double* resnorm, floa
   e = cudaStreamSynchronize(h->stream);
   if (e != cudaSuccess) return h->cuda_fail(e, "time integration");
   if ((rc = bounds_report(h))) return rc;
+  if ((rc = dma_report(h))) return rc;
   if (resnorm) {
     for (size_t i = 0; i < 4 * (size_t)nsteps; i++)
       if (!std::isfinite(resnorm[i])) return h->fail(FVS_ERR_NONFINITE, "residual norm is not finite at step " + std::to_string(i / 4 + 1));
@@ -911,6 +1000,7 @@ int fvs_profile_step(fvs_handle* h, int32_t cap, int32_t* n, char* names, float*
     ev.push_back(x);
     nm.push_back(label);
   };
+  if ((rc = refill_gather(h))) return rc;
   mark("start");
   K.begin_step(h->d, s);
   if (h->tile_mode == 1) {
@@ -918,6 +1008,12 @@ int fvs_profile_step(fvs_handle* h, int32_t cap, int32_t* n, char* names, float*
     for (size_t k = 0; k < h->stages.size(); k++) {
       K.tile_stage(dv, h->tv, h->stages[k], (int)k, s);
       mark("tile_stage");
+    }
+  } else if (h->tile_mode == 3) {
+    const DevView dv = h->tile_view();
+    for (size_t k = 0; k < h->stages.size(); k++) {
+      K.tile_dma_stage(dv, h->tv, h->dv, h->stages[k], (int)k, s);
+      mark("tile_dma_stage");
     }
   } else if (h->tile_mode == 2) {
     for (size_t k = 0; k < h->stages.size(); k++) {
@@ -990,6 +1086,13 @@ int fvs_tile_plan_info(const fvs_mesh* mesh, const fvs_options* opt, int32_t* in
   info[0] = P.ntiles; info[1] = P.lmax; info[2] = P.gmax; info[3] = P.fmax; info[4] = bad.empty() ? 1 : 0;
   info[5] = (int32_t)P.halo.size();
   if (!bad.empty()) { g_create_error = bad; return FVS_ERR_MESH; }
+  // the bulk-copy form's segments (mixed: 4-byte values)
+  TileDma D;
+  build_tile_dma(P, L.st_ptr, L.nc, D);
+  const std::string bad2 = check_tile_dma(P, D, 4, L.nc, L.st_cell.size());
+  const DmaSmem m = dma_smem(4, P.lmax, P.gmax, P.fmax, D.smax, D.pmax, D.rmax, D.qmax);
+  info[6] = (int32_t)m.total; info[7] = bad2.empty() ? 1 : 0;
+  if (!bad2.empty()) { g_create_error = "bulk-copy plan: " + bad2; return FVS_ERR_MESH; }
   return FVS_OK;
 }
 

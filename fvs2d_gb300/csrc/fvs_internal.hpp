@@ -185,6 +185,35 @@ struct TileView {
   size_t smem_bytes = 0;  // dynamic shared memory of one block
 };
 
+// Device view of a TileDma plan (fvs_tiles.hpp): the bulk-copy form of the
+// fused stage.  GB: the gather buffers the stages alternate between (the
+// same parity as TileView::Pbuf), coef: stencil coefficients in tile order
+// (pairs of the compute type); err: set when a bounded wait for the bulk
+// copies ran out.
+struct TileDmaView {
+  const int* gb0 = nullptr;
+  const int* sb0 = nullptr;
+  const int* pb0 = nullptr;
+  const int* rb0 = nullptr;
+  const int* cb0 = nullptr;
+  const uint16_t* lst = nullptr;
+  const uint16_t* lsp = nullptr;
+  const uint32_t* flr = nullptr;
+  const int2* lcf = nullptr;
+  const void* coef = nullptr;
+  const int* dptr = nullptr;
+  const int* dpos = nullptr;
+  void* GB[3] = {nullptr, nullptr, nullptr};
+  int smax = 0, pmax = 0, rmax = 0, qmax = 0;
+  int* err = nullptr;
+  size_t smem_bytes = 0;
+  // shared-memory regions of a block, byte offsets (fvs_tiles.hpp dma_smem):
+  // mbarrier at 0, primitives, face records, coefficients, stencil lists,
+  // stencil offsets, face cells, gather lists, gradients x / y, limiter,
+  // face fluxes
+  unsigned o_P = 0, o_Fg = 0, o_C = 0, o_L = 0, o_S = 0, o_R = 0, o_Q = 0, o_Gx = 0, o_Gy = 0, o_Ph = 0, o_F = 0;
+};
+
 struct StageParams {
   int stage = 1, nstages = 4, mode = MODE_RK, steady = 0, last = 0;
   double h = 0;       // h_rk(stage) (unsteady)
@@ -253,6 +282,14 @@ struct KernelSet {
   // face flux + RK update of stage k over the tiles (gradients from the
   // separate gradient kernel); d.Pv is the stage's input buffer
   cudaError_t (*tile_fu_stage)(const DevView&, const TileView&, const StageParams&, int k, cudaStream_t);
+  // bulk-copy fused stage (mixed build; null elsewhere), its shared memory
+  // for a plan (0: too large, or the build has none), and the fill of a
+  // gather buffer from the primitives (before the first stage after a new
+  // state)
+  cudaError_t (*tile_dma_stage)(const DevView&, const TileView&, const TileDmaView&, const StageParams&, int k,
+                                cudaStream_t);
+  size_t (*tile_dma_smem)(const TileView&, const TileDmaView&);
+  cudaError_t (*tile_dma_fill)(const DevView&, const TileDmaView&, int buf, cudaStream_t);
 };
 // Defect correction of a first-order steady batch (mixed build): per chunk
 // the FP64 residual R0 of the base state is evaluated once; the RK stages

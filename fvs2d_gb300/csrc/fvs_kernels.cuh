@@ -441,13 +441,14 @@ __device__ __forceinline__ void roe_flux_area_fp64(double gm1, double ggm1, cons
 // fills pj with the primitives of stencil entry k (global CSR index).
 // Shared by the separate gradient kernel (loads from global memory) and the
 // fused tile stage (loads from shared memory): the same arithmetic.
-template <int METHOD, int LIM, class Load>
-__device__ __forceinline__ void gradient_core(const DevView& d, int ic, const T* pc, Load load, T* gx, T* gy,
-                                              T& phi_out) {
+// gradient_core over the stencil entries [b, e) with coef(k) the (LSQ or
+// GG-cell) coefficient pair of entry k
+template <int METHOD, int LIM, class Load, class Coef>
+__device__ __forceinline__ void gradient_core_r(const DevView& d, int ic, const T* pc, int b, int e, Load load,
+                                                Coef coef, T* gx, T* gy, T& phi_out) {
   T pmin[4], pmax[4];
 #pragma unroll
   for (int v = 0; v < 4; v++) { pmin[v] = pc[v]; pmax[v] = pc[v]; }
-  const int b = d.st_ptr[ic], e = d.st_ptr[ic + 1];
   if (METHOD == FVS_GRAD_LSQ) {
     // grad_lsq, src/gradient_lsq.f90:393-401: sum over the stencil of
     // (coef * (p_j - p_i)) * w, stencil outer, variable inner
@@ -459,7 +460,7 @@ __device__ __forceinline__ void gradient_core(const DevView& d, int ic, const T*
     for (int k = b; k < e; k++) {
       T pj[4];
       load(k, pj);
-      const T2 c = ld2(d.st_coef, k);
+      const T2 c = coef(k);
 #if FVS_STRICT
       const T w = W[k];
 #endif
@@ -488,7 +489,7 @@ __device__ __forceinline__ void gradient_core(const DevView& d, int ic, const T*
     for (int k = b; k < e; k++) {
       T pj[4];
       load(k, pj);
-      const T2 c = ld2(d.st_coef, k);
+      const T2 c = coef(k);
 #pragma unroll
       for (int v = 0; v < 4; v++) { gx[v] = gx[v] + c.x * pj[v]; gy[v] = gy[v] + c.y * pj[v]; }
     }
@@ -553,6 +554,13 @@ __device__ __forceinline__ void gradient_core(const DevView& d, int ic, const T*
     }
     phi_out = phimin;
   }
+}
+
+template <int METHOD, int LIM, class Load>
+__device__ __forceinline__ void gradient_core(const DevView& d, int ic, const T* pc, Load load, T* gx, T* gy,
+                                              T& phi_out) {
+  gradient_core_r<METHOD, LIM>(d, ic, pc, d.st_ptr[ic], d.st_ptr[ic + 1], load,
+                               [&](int k) { return ld2(d.st_coef, k); }, gx, gy, phi_out);
 }
 
 template <int METHOD, int LIM, bool COH>
@@ -1043,9 +1051,9 @@ __device__ __forceinline__ void cell_residual_f(const DevView& d, int ic, bool w
 // the FP32 accumulator F, the accumulated residuals (SSP-RK(4,2), RK) or the
 // previous increment (SSP-RK3).  Per cell and SSP-RK3 step that is 192 bytes
 // of state traffic instead of 288 for writing U (and U0) at every stage.
-template <int MODE, bool COH>
-__device__ __forceinline__ void apply_stage_f(const DevView& d, const StageParams& sp, int ic, const float* res,
-                                              float ws, float* Pout, double* d2) {
+template <int MODE, bool COH, class Store>
+__device__ __forceinline__ void apply_stage_fs(const DevView& d, const StageParams& sp, int ic, const float* res,
+                                               float ws, Store store, double* d2) {
   float h = float(sp.h);
   if (sp.steady) {
     float dtl;
@@ -1108,11 +1116,18 @@ __device__ __forceinline__ void apply_stage_f(const DevView& d, const StageParam
   if (sp.last) st4(d.U, ic, u);
   float p[4];
   cons2prim(TP(gm1), u, p);
-  st4(Pout, ic, p);
+  store(p);
   if (sp.last) {
 #pragma unroll
     for (int v = 0; v < 4; v++) d2[v] += f2d_bits(inc[v] * inc[v]);
   }
+}
+
+// ... with the new primitives stored at Pout[ic]
+template <int MODE, bool COH>
+__device__ __forceinline__ void apply_stage_f(const DevView& d, const StageParams& sp, int ic, const float* res,
+                                              float ws, float* Pout, double* d2) {
+  apply_stage_fs<MODE, COH>(d, sp, ic, res, ws, [&](const float* p) { st4(Pout, ic, p); }, d2);
 }
 
 template <int MODE, bool COH>
@@ -1515,6 +1530,232 @@ static cudaError_t launch_tile_fu_stage(const DevView& d, const TileView& tv, co
   if (sp.mode == MODE_SSP3) return launch_tile_fu_mode<MODE_SSP3>(d, tv, sp, k, s);
   return launch_tile_fu_mode<MODE_RK>(d, tv, sp, k, s);
 }
+
+#if FVS_MIXED
+// ---------------------------------------------------------------------------
+// bulk-copy fused stage (FVS2D_TILE_STAGE=3; mixed, LSQ gradients)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// one bulk copy global -> shared, completing on the mbarrier (16-byte
+// aligned addresses, a multiple of 16 bytes; checked on the host)
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint32_t mbar) {
+  if (bytes == 0) return;
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
+                   smem_addr(dst)),
+               "l"(src), "r"(bytes), "r"(mbar)
+               : "memory");
+}
+
+// bounded wait for phase 0 of the mbarrier; false when the budget ran out
+__device__ __forceinline__ bool mbar_wait0(uint32_t mbar, long long budget) {
+  const long long t0 = clock64();
+  while (true) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(mbar)
+        : "memory");
+    if (done) return true;
+    if (clock64() - t0 > budget) return false;
+  }
+}
+
+// One RK stage of one tile with every input brought in by bulk copies:
+//  0. thread 0 arms the block's mbarrier with the byte count and issues one
+//     cp.async.bulk per segment (the tile's gather records of buffer kin,
+//     face records, coefficients, stencil lists and offsets, face cells,
+//     gather lists); every thread waits for them (bounded: after 2 s the
+//     block sets dv.err, waits once more for its copies and returns)
+//  2.-4. the phases of k_tile_stage, all operands in shared memory, with the
+//     same arithmetic (gradient_core_r, face_states, flux_eval, the ordered
+//     residual sum, apply_stage_fs); the new primitives of a cell go to every
+//     gather record of buffer kout that holds it (home and halos) and, at
+//     the last stage, to DevView::Pv
+template <int MODE, int REC, int LIM>
+__global__ void __launch_bounds__(256) k_tile_dma(const DevView d, const TileView tv, const TileDmaView dv,
+                                                 const StageParams sp, int kin, int kout) {
+  pdl_wait();
+  pdl_trigger();
+  extern __shared__ __align__(128) unsigned char dsm[];
+  const int t = blockIdx.x, tid = threadIdx.x, nthr = blockDim.x;
+  const int b = tv.c0[t], n = tv.c0[t + 1] - b;
+  const int hb = tv.h0[t], nl = n + (tv.h0[t + 1] - hb), ng = n + tv.nh1[t];
+  const int fb = tv.f0[t], nf = tv.f0[t + 1] - fb;
+  float* sP = reinterpret_cast<float*>(dsm + dv.o_P);
+  const float* sFg = reinterpret_cast<const float*>(dsm + dv.o_Fg);
+  const T2* sC = reinterpret_cast<const T2*>(dsm + dv.o_C);
+  const uint16_t* sL = reinterpret_cast<const uint16_t*>(dsm + dv.o_L);
+  const uint16_t* sS = reinterpret_cast<const uint16_t*>(dsm + dv.o_S);
+  const uint32_t* sR = reinterpret_cast<const uint32_t*>(dsm + dv.o_R);
+  const int2* sQ = reinterpret_cast<const int2*>(dsm + dv.o_Q);
+  float* sGx = reinterpret_cast<float*>(dsm + dv.o_Gx);
+  float* sGy = reinterpret_cast<float*>(dsm + dv.o_Gy);
+  float* sPh = reinterpret_cast<float*>(dsm + dv.o_Ph);
+  float* sF = reinterpret_cast<float*>(dsm + dv.o_F);
+  const uint32_t mbar = smem_addr(dsm);
+  const int s0 = dv.sb0[t], ns = dv.sb0[t + 1] - s0;
+  const int p0 = dv.pb0[t], np = dv.pb0[t + 1] - p0;
+  const int r0 = dv.rb0[t], nr = dv.rb0[t + 1] - r0;
+  const int q0 = dv.cb0[t], nq = dv.cb0[t + 1] - q0;
+  const int g0 = dv.gb0[t];
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(mbar) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
+  __syncthreads();
+  if (tid == 0) {
+    const uint32_t bytes = (uint32_t)(16 * nl + 32 * nf + 8 * ns + 2 * ns + 2 * np + 4 * nr + 8 * nq);
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(mbar), "r"(bytes) : "memory");
+    bulk_g2s(sP, static_cast<const float*>(dv.GB[kin]) + 4 * (size_t)g0, 16u * nl, mbar);
+    bulk_g2s((void*)sFg, static_cast<const float*>(tv.fgeo) + 8 * (size_t)fb, 32u * nf, mbar);
+    bulk_g2s((void*)sC, static_cast<const T2*>(dv.coef) + s0, 8u * ns, mbar);
+    bulk_g2s((void*)sL, dv.lst + s0, 2u * ns, mbar);
+    bulk_g2s((void*)sS, dv.lsp + p0, 2u * np, mbar);
+    bulk_g2s((void*)sR, dv.flr + r0, 4u * nr, mbar);
+    bulk_g2s((void*)sQ, dv.lcf + q0, 8u * nq, mbar);
+  }
+  if (!mbar_wait0(mbar, 4000000000ll)) {
+    // the copies are in flight: wait for them once more before leaving, so
+    // that no copy lands in shared memory after the block has exited
+    if (tid == 0) atomicExch(dv.err, 1);
+    mbar_wait0(mbar, 32000000000ll);
+    return;
+  }
+  // 2. gradients of the tile and halo1 cells (LSQ), from shared memory
+  if (REC != REC_FIRST) {
+    for (int i = tid; i < ng; i += nthr) {
+      const int gid = !LIM ? 0 : (i < n ? b + i : tv.halo[hb + i - n]);  // limiter data by device cell
+      auto load = [&](int k, float* pj) {
+        const float* q = sP + 4 * (int)sL[k];
+#pragma unroll
+        for (int v = 0; v < 4; v++) pj[v] = q[v];
+      };
+      auto coef = [&](int k) { return sC[k]; };
+      float gx[4], gy[4], ph = 1.f;
+      gradient_core_r<FVS_GRAD_LSQ, LIM>(d, gid, sP + 4 * i, (int)sS[i], (int)sS[i + 1], load, coef, gx, gy, ph);
+#pragma unroll
+      for (int v = 0; v < 4; v++) {
+        sGx[4 * i + v] = gx[v];
+        sGy[4 * i + v] = gy[v];
+      }
+      if (REC == REC_GENERAL) sPh[i] = LIM ? ph : static_cast<const float*>(d.phi)[i < n ? b + i : tv.halo[hb + i - n]];
+    }
+  }
+  __syncthreads();
+  // 3. face fluxes
+  const double time = d.tctl[1] + sp.dts;
+  for (int f = tid; f < nf; f += nthr) {
+    const uint32_t lr = sR[f];
+    const float* g = sFg + 8 * f;
+    const int l = (int)(lr & 0xFFFFu), rr = (int)(lr >> 16);
+    const bool interior = rr != 0xFFFF;
+    const int r = interior ? rr : l;
+    const int e = interior ? -1 : tv.face[fb + f];
+    const T2 nn = {g[0], g[1]};
+    const float af = g[2];
+    const T2 dl = {g[3], g[4]}, dr = {g[5], g[6]};
+    float pfL[4], pfR[4], flux[4], wsa;
+    const float phiL = REC == REC_GENERAL ? sPh[l] : 1.f, phiR = REC == REC_GENERAL ? sPh[r] : 1.f;
+    face_states<REC>(d, e, interior, time, nn, dl, dr, sP + 4 * l, sGx + 4 * l, sGy + 4 * l, phiL, sP + 4 * r,
+                     sGx + 4 * r, sGy + 4 * r, phiR, pfL, pfR);
+    flux_eval(d, pfL, pfR, nn, af, flux, wsa);
+#pragma unroll
+    for (int v = 0; v < 4; v++) sF[5 * f + v] = flux[v];
+    sF[5 * f + 4] = wsa;
+  }
+  __syncthreads();
+  // 4. gather, RK update, new primitives to every record of the cell
+  float* GBo = static_cast<float*>(dv.GB[kout]);
+  float* Pv = static_cast<float*>(d.Pv);
+  double d2[4] = {0.0, 0.0, 0.0, 0.0};
+  const bool want_ws = sp.steady && sp.stage == 1;
+  for (int i = tid; i < n; i += nthr) {
+    const int gid = b + i;
+    const int2 q = sQ[i];
+    const int sl[4] = {(int)(int16_t)(q.x & 0xFFFF), (int)(int16_t)((unsigned)q.x >> 16),
+                       (int)(int16_t)(q.y & 0xFFFF), (int)(int16_t)((unsigned)q.y >> 16)};
+    auto get = [&](int idx, float* f, float& w) {
+#pragma unroll
+      for (int v = 0; v < 4; v++) f[v] = sF[5 * idx + v];
+      w = sF[5 * idx + 4];
+    };
+    float res[4], ws;
+    residual_from_faces_f(sl, -static_cast<const float*>(d.volT)[gid], want_ws, get, res, ws);
+    const int j0 = dv.dptr[gid], j1 = dv.dptr[gid + 1];
+    apply_stage_fs<MODE, false>(d, sp, gid, res, ws, [&](const float* p) {
+      for (int j = j0; j < j1; j++) st4(GBo, dv.dpos[j], p);
+      if (sp.last) st4(Pv, gid, p);
+    }, d2);
+  }
+  if (sp.last) {
+    __syncthreads();  // the norm buffer reuses the gradient regions
+    stage_norms(d, d2, reinterpret_cast<double*>(dsm + dv.o_Gx));
+  }
+}
+
+// copies the primitives of every cell into its records of gather buffer buf
+__global__ void __launch_bounds__(256) k_dma_fill(const DevView d, const TileDmaView dv, int buf) {
+  pdl_wait();
+  pdl_trigger();
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= d.nc) return;
+  float p[4];
+  ld4(static_cast<const float*>(d.Pv), c, p);
+  float* G = static_cast<float*>(dv.GB[buf]);
+  for (int j = dv.dptr[c]; j < dv.dptr[c + 1]; j++) st4(G, dv.dpos[j], p);
+}
+
+template <int MODE>
+static cudaError_t launch_tile_dma_mode(const DevView& d, const TileView& tv, const TileDmaView& dv,
+                                        const StageParams& sp, int k, cudaStream_t s) {
+  const bool spec = d.khalf == 0.0 && d.omk == 1.0 && d.limiter == FVS_LIM_NONE;
+  const unsigned g = (unsigned)tv.ntiles;
+  const int ki = k % tv.nbuf, ko = (k + 1) % tv.nbuf;
+  if (d.first_order) launch_k(k_tile_dma<MODE, REC_FIRST, 0>, g, 256, dv.smem_bytes, s, d, tv, dv, sp, ki, ko);
+  else if (spec) launch_k(k_tile_dma<MODE, REC_SPEC, 0>, g, 256, dv.smem_bytes, s, d, tv, dv, sp, ki, ko);
+  else if (d.limiter != FVS_LIM_NONE)
+    launch_k(k_tile_dma<MODE, REC_GENERAL, 1>, g, 256, dv.smem_bytes, s, d, tv, dv, sp, ki, ko);
+  else launch_k(k_tile_dma<MODE, REC_GENERAL, 0>, g, 256, dv.smem_bytes, s, d, tv, dv, sp, ki, ko);
+  return cudaGetLastError();
+}
+
+static cudaError_t launch_tile_dma_stage(const DevView& d, const TileView& tv, const TileDmaView& dv,
+                                         const StageParams& sp, int k, cudaStream_t s) {
+  if (sp.mode == MODE_SSP42) return launch_tile_dma_mode<MODE_SSP42>(d, tv, dv, sp, k, s);
+  if (sp.mode == MODE_SSP3) return launch_tile_dma_mode<MODE_SSP3>(d, tv, dv, sp, k, s);
+  return launch_tile_dma_mode<MODE_RK>(d, tv, dv, sp, k, s);
+}
+
+static cudaError_t launch_tile_dma_fill(const DevView& d, const TileDmaView& dv, int buf, cudaStream_t s) {
+  launch_k(k_dma_fill, (unsigned)((d.nc + 255) / 256), 256, 0, s, d, dv, buf);
+  return cudaGetLastError();
+}
+
+// opts the instantiations in to dv.smem_bytes; returns it (0 if a block may
+// not have that much)
+static size_t tile_dma_smem(const TileView& tv, const TileDmaView& dv) {
+  (void)tv;
+  int dev = 0, cap = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&cap, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess)
+    return 0;
+  if (dv.smem_bytes + 64 > (size_t)cap) return 0;
+  const int b = (int)dv.smem_bytes;
+  bool ok = true;
+#define FVS_DMA_ATTR(M, R, L) \
+  ok = ok && cudaFuncSetAttribute(k_tile_dma<M, R, L>, cudaFuncAttributeMaxDynamicSharedMemorySize, b) == cudaSuccess
+  FVS_DMA_ATTR(MODE_SSP42, REC_FIRST, 0); FVS_DMA_ATTR(MODE_SSP42, REC_SPEC, 0);
+  FVS_DMA_ATTR(MODE_SSP42, REC_GENERAL, 0); FVS_DMA_ATTR(MODE_SSP42, REC_GENERAL, 1);
+  FVS_DMA_ATTR(MODE_SSP3, REC_FIRST, 0); FVS_DMA_ATTR(MODE_SSP3, REC_SPEC, 0);
+  FVS_DMA_ATTR(MODE_SSP3, REC_GENERAL, 0); FVS_DMA_ATTR(MODE_SSP3, REC_GENERAL, 1);
+  FVS_DMA_ATTR(MODE_RK, REC_FIRST, 0); FVS_DMA_ATTR(MODE_RK, REC_SPEC, 0);
+  FVS_DMA_ATTR(MODE_RK, REC_GENERAL, 0); FVS_DMA_ATTR(MODE_RK, REC_GENERAL, 1);
+#undef FVS_DMA_ATTR
+  return ok ? dv.smem_bytes : 0;
+}
+#endif  // FVS_MIXED
 
 // opts every instantiation in to the shared memory of the plan's largest
 // tile; returns the bytes of one block (0: more than a block may have)

@@ -260,4 +260,144 @@ inline std::string check_tile_plan(const TilePlan& P, int nc, int ne, const std:
   return std::string();
 }
 
+// ---------------------------------------------------------------------------
+// Bulk-copy form of the fused stage (FVS2D_TILE_STAGE=3)
+// ---------------------------------------------------------------------------
+// Every input of a tile block is one contiguous segment that a single
+// cp.async.bulk brings into shared memory: the primitives of the tile's
+// local cells (a gather buffer with one record per local cell, which every
+// stage fills for the next one: each cell's new primitives go to its home
+// record and to its record in every tile that holds it as a halo), the face
+// records, the stencil coefficients, local stencil lists, stencil offsets,
+// face cells and gather lists.  Each segment starts on a 16-byte boundary and
+// has a multiple of 16 bytes (the bulk copy's rule): entry counts are padded.
+struct TileDma {
+  std::vector<int> gb0;        // [ntiles + 1] gather segment, in cell records (4 values)
+  std::vector<int> sb0;        // [ntiles + 1] stencil entries (multiple of 8)
+  std::vector<int> pb0;        // [ntiles + 1] stencil offsets, uint16 (multiple of 8)
+  std::vector<int> rb0;        // [ntiles + 1] face cells, uint32 (multiple of 4)
+  std::vector<int> cb0;        // [ntiles + 1] gather lists, int2 (multiple of 2)
+  std::vector<uint16_t> lst;   // local cell of each stencil entry
+  std::vector<uint16_t> lsp;   // per gradient cell: first entry (ng + 1 values)
+  std::vector<uint32_t> flr;   // local L | local R << 16
+  std::vector<int2> lcf;       // per tile cell: four int16 signed local face refs
+  std::vector<int> coef_src;   // global stencil entry of each padded entry (-1: padding)
+  std::vector<int> dptr, dpos; // per device cell: its gather records (home first)
+  int smax = 0, pmax = 0, rmax = 0, qmax = 0;  // largest padded segment lengths
+};
+
+inline int pad_to(int n, int m) { return (n + m - 1) / m * m; }
+
+inline void build_tile_dma(const TilePlan& P, const std::vector<int>& st_ptr, int nc, TileDma& D) {
+  D = TileDma();
+  D.gb0.assign(1, 0); D.sb0.assign(1, 0); D.pb0.assign(1, 0); D.rb0.assign(1, 0); D.cb0.assign(1, 0);
+  std::vector<std::vector<int>> pos(nc);
+  for (int t = 0; t < P.ntiles; t++) {
+    const int b = P.c0[t], n = P.c0[t + 1] - b;
+    const int nh = P.h0[t + 1] - P.h0[t], nl = n + nh, ng = n + P.nh1[t];
+    const int nf = P.f0[t + 1] - P.f0[t], ns = P.s0[t + 1] - P.s0[t];
+    // gather records: home records first in each cell's list
+    for (int i = 0; i < nl; i++) {
+      const int c = i < n ? b + i : P.halo[P.h0[t] + i - n];
+      if (i < n) pos[c].insert(pos[c].begin(), D.gb0.back() + i);
+      else pos[c].push_back(D.gb0.back() + i);
+    }
+    D.gb0.push_back(D.gb0.back() + nl);
+    // stencil entries with their coefficients' global entry index
+    const int nsp = pad_to(ns, 8);
+    for (int k = 0; k < nsp; k++) D.lst.push_back(k < ns ? P.lst[P.s0[t] + k] : 0);
+    for (int i = 0; i < ng; i++) {
+      const int gid = i < n ? b + i : P.halo[P.h0[t] + i - n];
+      const int cnt = P.lsp[P.g0[t] + i + 1] - P.lsp[P.g0[t] + i];
+      for (int j = 0; j < cnt; j++) D.coef_src.push_back(st_ptr[gid] + j);
+    }
+    for (int k = ns; k < nsp; k++) D.coef_src.push_back(-1);
+    D.sb0.push_back(D.sb0.back() + nsp);
+    D.smax = std::max(D.smax, nsp);
+    const int npp = pad_to(ng + 1, 8);
+    for (int i = 0; i < npp; i++) D.lsp.push_back(i <= ng ? (uint16_t)P.lsp[P.g0[t] + i] : 0);
+    D.pb0.push_back(D.pb0.back() + npp);
+    D.pmax = std::max(D.pmax, npp);
+    const int nfp = pad_to(nf, 4);
+    for (int f = 0; f < nfp; f++) D.flr.push_back(f < nf ? P.flr[P.f0[t] + f] : 0u);
+    D.rb0.push_back(D.rb0.back() + nfp);
+    D.rmax = std::max(D.rmax, nfp);
+    const int nq = pad_to(n, 2);
+    for (int i = 0; i < nq; i++) D.lcf.push_back(i < n ? P.lcf[b + i] : make_int2(0, 0));
+    D.cb0.push_back(D.cb0.back() + nq);
+    D.qmax = std::max(D.qmax, nq);
+  }
+  D.dptr.assign(1, 0);
+  for (int c = 0; c < nc; c++) {
+    for (int q : pos[c]) D.dpos.push_back(q);
+    D.dptr.push_back((int)D.dpos.size());
+  }
+}
+
+// Shared-memory layout of a bulk-copy tile block, in bytes from the start
+// (every region on a 16-byte boundary).  R: bytes of one value (4 or 8).
+struct DmaSmem {
+  size_t mbar, P, Fg, C, L, S, Rr, Q, Gx, Gy, Ph, F, total;
+};
+inline size_t al16(size_t x) { return (x + 15) / 16 * 16; }
+inline DmaSmem dma_smem(int R, int lmax, int gmax, int fmax, int smax, int pmax, int rmax, int qmax) {
+  DmaSmem m;
+  size_t o = 0;
+  m.mbar = o; o += 16;
+  m.P = o; o = al16(o + (size_t)lmax * 4 * R);
+  m.Fg = o; o = al16(o + (size_t)fmax * 8 * R);
+  m.C = o; o = al16(o + (size_t)smax * 2 * R);
+  m.L = o; o = al16(o + (size_t)smax * 2);
+  m.S = o; o = al16(o + (size_t)pmax * 2);
+  m.Rr = o; o = al16(o + (size_t)rmax * 4);
+  m.Q = o; o = al16(o + (size_t)qmax * 8);
+  m.Gx = o; o = al16(o + (size_t)gmax * 4 * R);
+  m.Gy = o; o = al16(o + (size_t)gmax * 4 * R);
+  m.Ph = o; o = al16(o + (size_t)gmax * R);
+  m.F = o; o = al16(o + (size_t)fmax * 5 * R);
+  // the norm reduction reuses [Gx, ...) : at least 4 x 256 doubles
+  if (o - m.Gx < 4 * 256 * sizeof(double)) o = m.Gx + 4 * 256 * sizeof(double);
+  m.total = o;
+  return m;
+}
+
+// Checks what the bulk copies and the kernel's indexing rely on: segment
+// starts and byte sizes multiples of 16, segments within their arrays and
+// within the shared-memory regions, gather records within the buffer, every
+// stencil offset within the tile's entries.  Empty string when all hold.
+inline std::string check_tile_dma(const TilePlan& P, const TileDma& D, int R, int nc, size_t nstencil) {
+  auto bad = [](const char* what, int t) { return std::string(what) + " (tile " + std::to_string(t) + ")"; };
+  const int ntot = D.gb0.back();
+  for (int t = 0; t < P.ntiles; t++) {
+    const int n = P.c0[t + 1] - P.c0[t], nl = n + P.h0[t + 1] - P.h0[t], ng = n + P.nh1[t];
+    const int nf = P.f0[t + 1] - P.f0[t];
+    const int ns = D.sb0[t + 1] - D.sb0[t], np = D.pb0[t + 1] - D.pb0[t];
+    const int nr = D.rb0[t + 1] - D.rb0[t], nq = D.cb0[t + 1] - D.cb0[t];
+    if (D.gb0[t + 1] - D.gb0[t] != nl || nl > P.lmax) return bad("gather segment", t);
+    if (((size_t)D.gb0[t] * 4 * R) % 16 || ((size_t)nl * 4 * R) % 16) return bad("gather alignment", t);
+    if (((size_t)P.f0[t] * 8 * R) % 16 || nf > P.fmax) return bad("face record alignment", t);
+    if (ns % 8 || D.sb0[t] % 8 || ns > D.smax) return bad("stencil segment", t);
+    if (np % 8 || D.pb0[t] % 8 || np < ng + 1 || np > D.pmax) return bad("stencil offset segment", t);
+    if (nr % 4 || D.rb0[t] % 4 || nr < nf || nr > D.rmax) return bad("face cell segment", t);
+    if (nq % 2 || D.cb0[t] % 2 || nq < n || nq > D.qmax) return bad("gather list segment", t);
+    for (int i = 0; i <= ng; i++)
+      if (D.lsp[D.pb0[t] + i] > ns || (i > 0 && D.lsp[D.pb0[t] + i] < D.lsp[D.pb0[t] + i - 1]))
+        return bad("stencil offsets", t);
+    for (int k = 0; k < ns; k++) {
+      if (D.lst[D.sb0[t] + k] >= nl) return bad("stencil entry", t);
+      const int src = D.coef_src[D.sb0[t] + k];
+      if (src < -1 || src >= (int)nstencil) return bad("coefficient entry", t);
+    }
+    for (int f = 0; f < nf; f++)
+      if (D.flr[D.rb0[t] + f] != P.flr[P.f0[t] + f]) return bad("face cells", t);
+  }
+  if ((int)D.dptr.size() != nc + 1) return "gather record lists";
+  for (int c = 0; c < nc; c++) {
+    if (D.dptr[c + 1] <= D.dptr[c]) return "a cell without a home record";
+    for (int j = D.dptr[c]; j < D.dptr[c + 1]; j++)
+      if (D.dpos[j] < 0 || D.dpos[j] >= ntot) return "gather record outside the buffer";
+  }
+  return std::string();
+}
+
 }  // namespace fvs

@@ -247,9 +247,11 @@ int fvs_debug_set_gather(fvs_handle* h, int32_t cell, int32_t entry, int32_t val
 /* Host-only check of the fused stage's tile plan (no counterpart in the
  * reference; no GPU needed): builds the plan a mixed or double-float handle
  * would use for this mesh and checks every index its kernel derives from it.
- * info[6] = (tiles, largest local cell count, largest gradient cell count,
- * largest face count, 1 if every check holds, halo entries).  Returns
- * FVS_ERR_MESH (message in fvs_last_error(NULL)) on the first violation. */
+ * info[8] = (tiles, largest local cell count, largest gradient cell count,
+ * largest face count, 1 if every check holds, halo entries, shared memory of
+ * a block of the bulk-copy form in bytes (mixed), 1 if every alignment and
+ * extent of its copies holds).  Returns FVS_ERR_MESH (message in
+ * fvs_last_error(NULL)) on the first violation. */
 int fvs_tile_plan_info(const fvs_mesh* mesh, const fvs_options* opt, int32_t* info);
 /* Check of the FP64 kernels' reciprocal and square root (no counterpart in
  * the reference): for n host values x (positive normal numbers), out

@@ -48,14 +48,18 @@ def run(mesh, opt, mode, monkeypatch, steps=6):
     return launches, norms, u, r, w
 
 
-@pytest.mark.parametrize("mode", [1, 2])
+@pytest.mark.parametrize("mode", [1, 2, 3])
 @pytest.mark.parametrize("prec", [PREC_MIXED, PREC_FP64_DF])
 @pytest.mark.parametrize("name", sorted(CASES))
 def test_tile_stage_bit_identical_to_separate_kernels(name, prec, mode, monkeypatch):
     """mode 1: the whole stage in one launch per tile (k_tile_stage); mode 2:
     the gradient kernel, then face flux and update in one launch per tile
-    (k_tile_flux_update)."""
+    (k_tile_flux_update); mode 3: the whole stage per tile with its inputs
+    brought into shared memory by bulk copies (k_tile_dma; mixed precision,
+    LSQ gradients)."""
     mesh, opt = CASES[name]()
+    if mode == 3 and (prec != PREC_MIXED or opt.grad_method != 3):
+        pytest.skip("the bulk-copy form covers mixed precision with LSQ gradients")
     opt = opt.replace(precision=prec)
     lf, nf, uf, rf, wf = run(mesh, opt, mode, monkeypatch)
     ls, ns, us, rs, ws = run(mesh, opt, 0, monkeypatch)
@@ -63,7 +67,7 @@ def test_tile_stage_bit_identical_to_separate_kernels(name, prec, mode, monkeypa
     grad = 0 if opt.reconst == 1 else 1
     # k_begin_step + per stage one fused launch (mode 1) or gradient + one
     # launch (mode 2)
-    assert lf == 1 + nst * (1 if mode == 1 else grad + 1), lf
+    assert lf == 1 + nst * (1 if mode in (1, 3) else grad + 1), lf
     assert ls > lf
     assert np.array_equal(uf, us), float(np.abs(uf - us).max())
     assert np.array_equal(rf, rs) and np.array_equal(wf, ws)

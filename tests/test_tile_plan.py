@@ -1,8 +1,10 @@
-"""Tile plans of the fused RK stage, checked on the CPU (no GPU): every
-index the fused kernel derives from the plan (local cells, stencil
+"""Tile plans of the fused RK stages, checked on the CPU (no GPU): every
+index the fused kernels derive from the plan (local cells, stencil
 entries, faces, gather entries) lies within the shared-memory extents and
-device arrays it indexes (fvs_tile_plan_info runs check_tile_plan), and the
-shared memory of the largest tile stays within a block's limit."""
+device arrays it indexes (fvs_tile_plan_info runs check_tile_plan), every
+bulk copy of the bulk-copy form starts on a 16-byte boundary with a multiple
+of 16 bytes and stays within its array (check_tile_dma), and the shared
+memory of the largest tile stays within a block's limit."""
 import ctypes as C
 import os
 
@@ -21,7 +23,7 @@ def plan(mesh, opt):
     lib = capi.load()
     m = capi.MeshArrays(mesh)
     o = opt.to_struct()
-    info = np.zeros(6, np.int32)
+    info = np.zeros(8, np.int32)
     rc = lib.fvs_tile_plan_info(C.byref(m.struct), C.byref(o), capi.ptr(info))
     assert rc == capi.FVS_OK, lib.fvs_last_error(None).decode()
     return info
@@ -48,8 +50,10 @@ def test_tile_plan_indices_within_bounds(name):
         opt = cases.periodic_vortex(4)[1]
     else:
         mesh, opt = CASES[name]()
-    ntiles, lmax, gmax, fmax, ok, nhalo = plan(mesh, opt)
-    assert ok == 1
+    ntiles, lmax, gmax, fmax, ok, nhalo, dma_smem, dma_ok = plan(mesh, opt)
+    assert ok == 1 and dma_ok == 1
+    # the bulk-copy form's block (mixed) fits a block's shared memory
+    assert dma_smem <= SMEM_OPTIN, dma_smem
     assert ntiles >= 1 and ntiles <= -(-mesh.ncells // (TILE_CELLS // 2))
     assert gmax <= lmax
     # shared memory of one tile block in the double-float build (8-byte
