@@ -1566,7 +1566,7 @@ __device__ __forceinline__ bool mbar_wait0(uint32_t mbar, long long budget) {
 //  0. thread 0 arms the block's mbarrier with the byte count and issues one
 //     cp.async.bulk per segment (the tile's gather records of buffer kin,
 //     face records, coefficients, stencil lists and offsets, face cells,
-//     gather lists); every thread waits for them (bounded: after 2 s the
+//     gather lists); every thread waits for them (bounded: after ~0.5 s the
 //     block sets dv.err, waits once more for its copies and returns)
 //  2.-4. the phases of k_tile_stage, all operands in shared memory, with the
 //     same arithmetic (gradient_core_r, face_states, flux_eval, the ordered
@@ -1616,11 +1616,11 @@ __global__ void __launch_bounds__(256) k_tile_dma(const DevView d, const TileVie
     bulk_g2s((void*)sR, dv.flr + r0, 4u * nr, mbar);
     bulk_g2s((void*)sQ, dv.lcf + q0, 8u * nq, mbar);
   }
-  if (!mbar_wait0(mbar, 4000000000ll)) {
+  if (!mbar_wait0(mbar, 1000000000ll)) {
     // the copies are in flight: wait for them once more before leaving, so
     // that no copy lands in shared memory after the block has exited
     if (tid == 0) atomicExch(dv.err, 1);
-    mbar_wait0(mbar, 32000000000ll);
+    mbar_wait0(mbar, 2000000000ll);
     return;
   }
   // 2. gradients of the tile and halo1 cells (LSQ), from shared memory
