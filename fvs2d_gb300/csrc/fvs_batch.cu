@@ -248,6 +248,7 @@ void set_batch_stages(fvs_batch* B) {
       static const double A[4] = {0, 0.0, 0.75, 1.0 / 3.0}, Bw[4] = {0, 1.0, 0.25, 2.0 / 3.0};
       sp.a = A[k]; sp.b = Bw[k];
     }
+    sp.set_pairs();
     B->stages.push_back(sp);
   }
   B->d.dt = o.dt;

@@ -380,6 +380,7 @@ void set_stages(fvs_handle* H) {
       static const double A[4] = {0, 0.0, 0.75, 1.0 / 3.0}, B[4] = {0, 1.0, 0.25, 2.0 / 3.0};
       sp.a = A[k]; sp.b = B[k];
     }
+    sp.set_pairs();
     H->stages.push_back(sp);
   }
   H->d.dt = H->dt;
@@ -624,6 +625,10 @@ int fvs_create(const fvs_mesh* mesh, const fvs_options* opt, fvs_handle** out) {
     rc = H->mixed ? build_device<float>(H.get()) : H->df ? build_device<df64>(H.get()) : build_device<double>(H.get());
   }
   if (rc) { g_create_error = H->err; return rc; }
+  if (H->ks->update_wave) {
+    const int ns = H->o.rk_nstages;
+    d.upd_grid = H->ks->update_wave((ns == 3 && H->o.ssprk) ? MODE_SSP3 : (H->o.ssprk ? MODE_SSP42 : MODE_RK));
+  }
   if (H->bounds) {
     void* p = nullptr;
     if (!H->arena.alloc(p, 4 * sizeof(int))) { g_create_error = "bounds word allocation failed"; return FVS_ERR_NOMEM; }

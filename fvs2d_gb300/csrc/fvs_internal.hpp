@@ -131,6 +131,8 @@ struct DevView {
   int norm_cap = 0;
   int* bounds_err = nullptr;      // [4] index-checking kernels: flag, site, index, extent
   int* stepctl = nullptr;         // [0] = steps done in this call
+  int upd_grid = 0;               // blocks of the last stage's update launch, which strides over the cells
+                                  // (one wave of resident blocks; 0: one block per 256 cells)
   double* tctl = nullptr;         // [0] = t1, [1] = told of the current step
   // scheme
   double gamma = 1.4, khalf = 0, nkhalf = 0, omk = 1, cfl = 1, dt = 0;
@@ -221,6 +223,17 @@ struct StageParams {
   double coef = 1;    // rk_coef(stage)
   double a = 0, b = 1;  // SSP3 Shu-Osher weights
   double dts = 0;     // stage time offset from told
+  // h, cst, coef, a, b as pairs of FP32 numbers (hi, lo) for the
+  // double-float update; set_pairs() fills them from the doubles
+  float hp[2] = {0, 0}, cstp[2] = {0, 0}, coefp[2] = {1, 0}, ap[2] = {0, 0}, bp[2] = {1, 0};
+  void set_pairs() {
+    const double src[5] = {h, cst, coef, a, b};
+    float* dst[5] = {hp, cstp, coefp, ap, bp};
+    for (int i = 0; i < 5; i++) {
+      dst[i][0] = (float)src[i];
+      dst[i][1] = (float)(src[i] - (double)dst[i][0]);
+    }
+  }
 };
 
 // Software grid barrier of the persistent kernel.  Every wait is bounded by a
@@ -290,6 +303,9 @@ struct KernelSet {
                                 cudaStream_t);
   size_t (*tile_dma_smem)(const TileView&, const TileDmaView&);
   cudaError_t (*tile_dma_fill)(const DevView&, const TileDmaView&, int buf, cudaStream_t);
+  // blocks of 256 threads of the update kernel of an RK mode resident on the
+  // device at once (0: unknown); queried before any graph capture
+  int (*update_wave)(int mode);
 };
 // Defect correction of a first-order steady batch (mixed build): per chunk
 // the FP64 residual R0 of the base state is evaluated once; the RK stages

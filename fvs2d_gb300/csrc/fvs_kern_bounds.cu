@@ -13,7 +13,8 @@ const KernelSet& kernels_fp64_bounds() {
   static const KernelSet k = {"fp64_bounds", k_bounds::launch_begin_step, k_bounds::launch_cvar2pvar,
                               k_bounds::launch_gradient, k_bounds::launch_flux, k_bounds::launch_update,
                               k_bounds::launch_residual_out, k_bounds::persistent_occupancy,
-                              k_bounds::launch_persistent, k_bounds::launch_tiled_step, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+                              k_bounds::launch_persistent, k_bounds::launch_tiled_step, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
+                              k_bounds::update_wave};
   return k;
 }
 }  // namespace fvs

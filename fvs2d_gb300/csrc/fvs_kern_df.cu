@@ -13,7 +13,8 @@ const KernelSet& kernels_fp64_df() {
   static const KernelSet k = {"fp64_df", k_df::launch_begin_step, k_df::launch_cvar2pvar, k_df::launch_gradient,
                               k_df::launch_flux, k_df::launch_update, k_df::launch_residual_out, k_df::persistent_occupancy, k_df::launch_persistent, k_df::launch_tiled_step,
                               k_df::launch_tile_stage, k_df::tile_smem,
-                              k_df::launch_tile_fu_stage, nullptr, nullptr, nullptr};
+                              k_df::launch_tile_fu_stage, nullptr, nullptr, nullptr,
+                              k_df::update_wave};
   return k;
 }
 }  // namespace fvs

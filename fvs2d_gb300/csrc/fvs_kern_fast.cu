@@ -10,7 +10,8 @@ const KernelSet& kernels_fp64_fast() {
   static const KernelSet k = {"fast", k_fast::launch_begin_step, k_fast::launch_cvar2pvar, k_fast::launch_gradient,
                               k_fast::launch_flux, k_fast::launch_update, k_fast::launch_residual_out, k_fast::persistent_occupancy,
                               k_fast::launch_persistent, k_fast::launch_tiled_step,
-                              nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+                              nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
+                              k_fast::update_wave};
   return k;
 }
 }  // namespace fvs

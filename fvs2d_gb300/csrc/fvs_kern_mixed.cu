@@ -13,7 +13,8 @@ const KernelSet& kernels_mixed() {
                               k_mixed::launch_persistent, k_mixed::launch_tiled_step,
                               k_mixed::launch_tile_stage, k_mixed::tile_smem,
                               k_mixed::launch_tile_fu_stage, k_mixed::launch_tile_dma_stage,
-                              k_mixed::tile_dma_smem, k_mixed::launch_tile_dma_fill};
+                              k_mixed::tile_dma_smem, k_mixed::launch_tile_dma_fill,
+                              k_mixed::update_wave};
   return k;
 }
 const DcKernels& dc_kernels() {

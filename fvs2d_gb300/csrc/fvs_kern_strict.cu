@@ -11,7 +11,8 @@ const KernelSet& kernels_fp64_strict() {
   static const KernelSet k = {"strict", k_strict::launch_begin_step, k_strict::launch_cvar2pvar, k_strict::launch_gradient,
                               k_strict::launch_flux, k_strict::launch_update, k_strict::launch_residual_out, k_strict::persistent_occupancy,
                               k_strict::launch_persistent, k_strict::launch_tiled_step,
-                              nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+                              nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
+                              k_strict::update_wave};
   return k;
 }
 }  // namespace fvs

@@ -879,12 +879,10 @@ __device__ __forceinline__ void cell_residual(const DevView& d, int ic, double* 
 // df64 value as FP64: two exact conversions on the integer pipe, one exact add
 __device__ __forceinline__ double to_double(df64 x) { return f2d_bits(x.hi) + f2d_bits(x.lo); }
 
-// df64 flux slots summed in df64 in the reference's order, times 1/vol in
-// df64, then one FP64 addition per component
-// flux records of a cell's faces in its gather order (see
-// residual_from_faces_f), summed in df64, times -1/vol in df64
+// df64 flux records of a cell's faces summed in df64 in its gather order
+// (the reference's order; see residual_from_faces_f), times -1/vol in df64
 template <bool WS, class Get>
-__device__ __forceinline__ void residual_from_faces_df(const int* sl, df64 rv, Get get, double* res, double& ws) {
+__device__ __forceinline__ void residual_from_faces_df(const int* sl, df64 rv, Get get, df64* res, double& ws) {
   df64 r[4] = {df64(0.f, 0.f), df64(0.f, 0.f), df64(0.f, 0.f), df64(0.f, 0.f)}, w(0.f, 0.f);
 #pragma unroll
   for (int j = 0; j < 4; j++) {
@@ -898,12 +896,12 @@ __device__ __forceinline__ void residual_from_faces_df(const int* sl, df64 rv, G
     if (WS) w = w + wf;
   }
 #pragma unroll
-  for (int v = 0; v < 4; v++) res[v] = to_double(r[v] * rv);
+  for (int v = 0; v < 4; v++) res[v] = r[v] * rv;
   ws = WS ? to_double(w) : 0.0;
 }
 
 template <bool WS, bool COH>
-__device__ __forceinline__ void cell_residual(const DevView& d, int ic, double* res, double& ws) {
+__device__ __forceinline__ void cell_residual_df(const DevView& d, int ic, df64* res, double& ws) {
   const int4 cf = d.cflist[ic];
   const int sl[4] = {cf.x, cf.y, cf.z, cf.w};
   const df64 rv = -static_cast<const df64*>(d.volT)[ic];
@@ -911,6 +909,15 @@ __device__ __forceinline__ void cell_residual(const DevView& d, int ic, double* 
     ldc4<COH>(static_cast<const df64*>(d.eflux), idx, f);
     if (WS) w = ldc1<COH>(static_cast<const df64*>(d.ews), idx);
   }, res, ws);
+}
+
+// ... as FP64 (one exact FP64 addition per component)
+template <bool WS, bool COH>
+__device__ __forceinline__ void cell_residual(const DevView& d, int ic, double* res, double& ws) {
+  df64 r[4];
+  cell_residual_df<WS, COH>(d, ic, r, ws);
+#pragma unroll
+  for (int v = 0; v < 4; v++) res[v] = to_double(r[v]);
 }
 #else
 template <bool WS, bool COH>
@@ -950,6 +957,17 @@ __device__ __forceinline__ void cell_residual(const DevView& d, int ic, double* 
 }
 #endif
 
+#if FVS_DF
+// primitives from a double-float conservative state
+__device__ __forceinline__ void cons2prim_df(df64 g, const df64* u, df64* p) {
+  const df64 r = u[0], ri = df64(1) / r;
+  p[0] = r;
+  p[1] = u[1] * ri;
+  p[2] = u[2] * ri;
+  p[3] = g * (u[3] - df64(0.5) * r * (p[1] * p[1] + p[2] * p[2]));
+}
+#endif
+
 // g = gamma - 1 in the compute type
 __device__ __forceinline__ void cons2prim(T g, const double* u, T* p) {
 #if FVS_MIXED
@@ -959,11 +977,8 @@ __device__ __forceinline__ void cons2prim(T g, const double* u, T* p) {
   p[2] = d2f_bits(u[2]) * ri;
   p[3] = g * (d2f_bits(u[3]) - 0.5f * r * (p[1] * p[1] + p[2] * p[2]));
 #elif FVS_DF
-  const df64 r = df_from_double(u[0]), ri = df64(1) / r;
-  p[0] = r;
-  p[1] = df_from_double(u[1]) * ri;
-  p[2] = df_from_double(u[2]) * ri;
-  p[3] = g * (df_from_double(u[3]) - df64(0.5) * r * (p[1] * p[1] + p[2] * p[2]));
+  const df64 ud[4] = {df_from_double(u[0]), df_from_double(u[1]), df_from_double(u[2]), df_from_double(u[3])};
+  cons2prim_df(g, ud, p);
 #elif !FVS_STRICT
   const double ri = rcp_nr(u[0]);
   p[0] = u[0];
@@ -1002,6 +1017,79 @@ __device__ __forceinline__ void block_sum4(const double* v, double* out) {
   __shared__ double sh[4 * 256];
   block_sum4_in(v, out, sh);
 }
+
+// Per-thread sums of the squared increments |U - U0|^2 (the RMS(dU)
+// partials).  Mixed precision and double-float: summed as unevaluated pairs
+// hi + lo of FP32 numbers (about 48 significant bits, all terms
+// non-negative) on the FP32 pipe; mixed adds FP32 squares by TwoSum,
+// double-float adds the double-float squares of its increments.  GB300's FP64
+// pipe does 2 lane operations per clock and SM: FP64 sums of 4 squares per
+// cell and a shared-memory FP64 tree per block made the last stage's mixed
+// update kernel 2.8x as long as the others (65 against 23 us at 1,048,576
+// cells).  The FP64 builds keep FP64 sums.
+#if FVS_MIXED || FVS_DF
+// (h, l) += (h2, l2) for non-negative pairs: TwoSum of the high parts, the
+// low parts added to its error, renormalised (Fast2Sum)
+__device__ __forceinline__ void pair_add(float& h, float& l, float h2, float l2) {
+  const float s = h + h2, bp = s - h;
+  const float e = ((h - (s - bp)) + (h2 - bp)) + (l + l2);
+  h = s + e;
+  l = e - (h - s);
+}
+struct NormAcc {
+  float h[4] = {0.f, 0.f, 0.f, 0.f}, l[4] = {0.f, 0.f, 0.f, 0.f};
+#if FVS_MIXED
+  __device__ __forceinline__ void add(int v, float x) { two_sum(h[v], l[v], x); }
+#else
+  __device__ __forceinline__ void add(int v, df64 x) { pair_add(h[v], l[v], x.hi, x.lo); }
+#endif
+  __device__ __forceinline__ void to_double(double* o) const {
+#pragma unroll
+    for (int v = 0; v < 4; v++) o[v] = f2d_bits(h[v]) + f2d_bits(l[v]);
+  }
+};
+// the block's sums per component into thread 0's a, in a fixed order (lanes
+// by shuffle-down, then the warps in index order); sh: 32 x 4 float2
+__device__ __forceinline__ void block_pairs4(NormAcc& a, float2* sh) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+  for (int v = 0; v < 4; v++)
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const float h2 = __shfl_down_sync(0xffffffffu, a.h[v], o), l2 = __shfl_down_sync(0xffffffffu, a.l[v], o);
+      pair_add(a.h[v], a.l[v], h2, l2);
+    }
+  if (lane == 0)
+#pragma unroll
+    for (int v = 0; v < 4; v++) sh[4 * w + v] = make_float2(a.h[v], a.l[v]);
+  __syncthreads();
+  if (w == 0) {
+#pragma unroll
+    for (int v = 0; v < 4; v++) {
+      const float2 p = lane < nw ? sh[4 * lane + v] : make_float2(0.f, 0.f);
+      a.h[v] = p.x;
+      a.l[v] = p.y;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const float h2 = __shfl_down_sync(0xffffffffu, a.h[v], o), l2 = __shfl_down_sync(0xffffffffu, a.l[v], o);
+        pair_add(a.h[v], a.l[v], h2, l2);
+      }
+    }
+  }
+  __syncthreads();
+}
+#define FVS_NORM_SH_BYTES (32 * 4 * 8)
+#else
+struct NormAcc {
+  double s[4] = {0.0, 0.0, 0.0, 0.0};
+  __device__ __forceinline__ void add(int v, double x) { s[v] += x; }
+  __device__ __forceinline__ void to_double(double* o) const {
+#pragma unroll
+    for (int v = 0; v < 4; v++) o[v] = s[v];
+  }
+};
+#define FVS_NORM_SH_BYTES (4 * 256 * 8)
+#endif
 
 #if FVS_MIXED
 // Mixed precision: the slot sums are exact (TwoSum) and the state stays FP64,
@@ -1053,7 +1141,7 @@ __device__ __forceinline__ void cell_residual_f(const DevView& d, int ic, bool w
 // of state traffic instead of 288 for writing U (and U0) at every stage.
 template <int MODE, bool COH, class Store>
 __device__ __forceinline__ void apply_stage_fs(const DevView& d, const StageParams& sp, int ic, const float* res,
-                                               float ws, Store store, double* d2) {
+                                               float ws, Store store, NormAcc& na) {
   float h = float(sp.h);
   if (sp.steady) {
     float dtl;
@@ -1119,31 +1207,31 @@ __device__ __forceinline__ void apply_stage_fs(const DevView& d, const StagePara
   store(p);
   if (sp.last) {
 #pragma unroll
-    for (int v = 0; v < 4; v++) d2[v] += f2d_bits(inc[v] * inc[v]);
+    for (int v = 0; v < 4; v++) na.add(v, inc[v] * inc[v]);
   }
 }
 
 // ... with the new primitives stored at Pout[ic]
 template <int MODE, bool COH>
 __device__ __forceinline__ void apply_stage_f(const DevView& d, const StageParams& sp, int ic, const float* res,
-                                              float ws, float* Pout, double* d2) {
-  apply_stage_fs<MODE, COH>(d, sp, ic, res, ws, [&](const float* p) { st4(Pout, ic, p); }, d2);
+                                              float ws, float* Pout, NormAcc& na) {
+  apply_stage_fs<MODE, COH>(d, sp, ic, res, ws, [&](const float* p) { st4(Pout, ic, p); }, na);
 }
 
 template <int MODE, bool COH>
-__device__ __forceinline__ void update_item(const DevView& d, const StageParams& sp, int ic, double* d2) {
+__device__ __forceinline__ void update_item(const DevView& d, const StageParams& sp, int ic, NormAcc& na) {
   float res[4], ws;
   cell_residual_f(d, ic, sp.steady && sp.stage == 1, res, ws);
-  apply_stage_f<MODE, COH>(d, sp, ic, res, ws, static_cast<float*>(d.Pv), d2);
+  apply_stage_f<MODE, COH>(d, sp, ic, res, ws, static_cast<float*>(d.Pv), na);
 }
 
 #else
 // the RK stage of one cell from its residual res (and, at a steady first
 // stage, its wave-speed sum ws); the new primitives go to Pout; at the last
-// stage adds |U-U0|^2 to d2
+// stage adds |U-U0|^2 to na
 template <int MODE, bool COH>
 __device__ __forceinline__ void apply_stage_d(const DevView& d, const StageParams& sp, int ic, const double* res,
-                                              double ws, T* Pout, double* d2) {
+                                              double ws, T* Pout, NormAcc& na) {
   {
     double h = sp.h;
     if (sp.steady) {
@@ -1205,32 +1293,147 @@ __device__ __forceinline__ void apply_stage_d(const DevView& d, const StageParam
 #pragma unroll
       for (int v = 0; v < 4; v++) {
         const double dd = fabs(u[v] - u0[v]);
-        d2[v] += dd * dd;
+        na.add(v, dd * dd);
       }
     }
   }
 }
 
-// one cell of an RK stage; at the last stage adds |U-U0|^2 to d2
+#if FVS_DF
+// The RK stage of one cell in double-float arithmetic (the double-float
+// build): the residual arrives as df64, the state is read as FP64 and split
+// exactly on the integer pipe (df_from_double), the stage is formed in df64
+// on the FP32 pipe (relative error ~2^-48 per operation, against 2^-53 in
+// FP64), and the new state is written as FP64 (one exact addition per
+// component).  The accumulator F holds df64 pairs in the same 8 bytes per
+// component; U0 stays FP64.  The same formulas and order as apply_stage_d:
+// src/runge_kutta.f90:225-226 / :383-387 (SSP-RK(4,2)), :156-162 / :302-313
+// (RK), and the SSP-RK3 extension.  Per cell and stage the FP64 pipe is left
+// with the four additions of the state store.
 template <int MODE, bool COH>
-__device__ __forceinline__ void update_item(const DevView& d, const StageParams& sp, int ic, double* d2) {
+__device__ __forceinline__ void apply_stage_df(const DevView& d, const StageParams& sp, int ic, const df64* res,
+                                               double ws, T* Pout, NormAcc& na) {
+  df64 h(sp.hp[0], sp.hp[1]);
+  if (sp.steady) {
+    double dtl;
+    if (sp.stage == 1) {  // compute_local_time, src/runge_kutta.f90:424-437
+      dtl = d.cfl * d.vol[ic] / (0.5 * ws);
+      d.dtl[ic] = dtl;
+    } else {
+      dtl = ldc1<COH>(d.dtl, ic);
+    }
+    h = df_from_double(dtl) * df64(sp.cstp[0], sp.cstp[1]);
+  }
+  double ud[4];
+  df64 u0[4], u[4], f[4];
+  df64* F = reinterpret_cast<df64*>(d.F);
+  if (sp.stage == 1) {
+    ldc4<COH>(d.U, ic, ud);
+    st4(d.U0, ic, ud);
+#pragma unroll
+    for (int v = 0; v < 4; v++) f[v] = df64(0.f, 0.f);
+  } else {
+    ldc4<COH>(d.U0, ic, ud);
+    if (MODE != MODE_SSP3) ldc4<COH>(F, ic, f);
+  }
+#pragma unroll
+  for (int v = 0; v < 4; v++) u0[v] = df_from_double(ud[v]);
+  const df64 c(sp.coefp[0], sp.coefp[1]);
+  if (MODE == MODE_SSP42) {
+#pragma unroll
+    for (int v = 0; v < 4; v++) {
+      u[v] = u0[v] + h * (c * res[v] + f[v]);
+      f[v] = f[v] + res[v];
+    }
+    if (!sp.last) st4(F, ic, f);
+  } else if (MODE == MODE_RK) {
+#pragma unroll
+    for (int v = 0; v < 4; v++) {
+      f[v] = f[v] + c * res[v];
+      u[v] = u0[v] + h * (sp.last ? f[v] : res[v]);
+    }
+    if (!sp.last) st4(F, ic, f);
+  } else {
+    df64 cur[4];
+    if (sp.stage == 1) {
+#pragma unroll
+      for (int v = 0; v < 4; v++) cur[v] = u0[v];
+    } else {
+      double cd[4];
+      ldc4<COH>(d.U, ic, cd);
+#pragma unroll
+      for (int v = 0; v < 4; v++) cur[v] = df_from_double(cd[v]);
+    }
+    const df64 a(sp.ap[0], sp.ap[1]), b(sp.bp[0], sp.bp[1]);
+#pragma unroll
+    for (int v = 0; v < 4; v++) {
+      const df64 st = cur[v] + h * res[v];
+      u[v] = sp.stage == 1 ? st : a * u0[v] + b * st;
+    }
+  }
+  // the stored state is exactly the df64 value (48 significant bits)
+  double uo[4];
+#pragma unroll
+  for (int v = 0; v < 4; v++) uo[v] = to_double(u[v]);
+  st4(d.U, ic, uo);
+  T p[4];
+  cons2prim_df(TP(gm1), u, p);
+  st4(Pout, ic, p);
+  if (sp.last) {
+#pragma unroll
+    for (int v = 0; v < 4; v++) {
+      const df64 dd = u[v] - u0[v];
+      na.add(v, dd * dd);
+    }
+  }
+}
+
+// one cell of an RK stage; at the last stage adds |U-U0|^2 to na
+template <int MODE, bool COH>
+__device__ __forceinline__ void update_item(const DevView& d, const StageParams& sp, int ic, NormAcc& na) {
+  df64 res[4];
+  double ws;
+  if (sp.steady && sp.stage == 1) cell_residual_df<true, COH>(d, ic, res, ws);
+  else cell_residual_df<false, COH>(d, ic, res, ws);
+  apply_stage_df<MODE, COH>(d, sp, ic, res, ws, static_cast<T*>(d.Pv), na);
+}
+#else
+// one cell of an RK stage; at the last stage adds |U-U0|^2 to na
+template <int MODE, bool COH>
+__device__ __forceinline__ void update_item(const DevView& d, const StageParams& sp, int ic, NormAcc& na) {
   double res[4], ws;
   if (sp.steady && sp.stage == 1) cell_residual<true, COH>(d, ic, res, ws);
   else cell_residual<false, COH>(d, ic, res, ws);
-  apply_stage_d<MODE, COH>(d, sp, ic, res, ws, static_cast<T*>(d.Pv), d2);
+  apply_stage_d<MODE, COH>(d, sp, ic, res, ws, static_cast<T*>(d.Pv), na);
 }
+#endif
 
 #endif  // FVS_MIXED
 
-// RMS of |U - U0| per component from the block partials, by one block of
-// 256 threads in a fixed order (deterministic); advances the step counter
-__device__ __forceinline__ void norm_final_block(const DevView& d, double* sh) {
+// RMS of |U - U0| per component from the block partials, by one block in a
+// fixed order (deterministic); advances the step counter.  sh: the shared
+// memory of the block sums (FVS_NORM_SH_BYTES)
+__device__ __forceinline__ void norm_final_block(const DevView& d, void* sh) {
+  double out[4];
+#if FVS_MIXED || FVS_DF
+  NormAcc a;
+  const float2* P = reinterpret_cast<const float2*>(d.partials);
+#pragma unroll 4
+  for (int i = threadIdx.x; i < d.nblk_red; i += blockDim.x)
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      const float2 q = __ldcg(P + 4 * (size_t)i + k);
+      pair_add(a.h[k], a.l[k], q.x, q.y);
+    }
+  block_pairs4(a, static_cast<float2*>(sh));
+  a.to_double(out);
+#else
   double s[4] = {0.0, 0.0, 0.0, 0.0};
   for (int i = threadIdx.x; i < d.nblk_red; i += blockDim.x)
 #pragma unroll
     for (int k = 0; k < 4; k++) s[k] += __ldcg(d.partials + 4 * i + k);
-  double out[4];
-  block_sum4_in(s, out, sh);
+  block_sum4_in(s, out, static_cast<double*>(sh));
+#endif
   if (threadIdx.x == 0) {
     const int istep = d.stepctl[0] + 1;
     double* o = d.norms + 4 * (size_t)((istep - 1) % d.norm_cap);
@@ -1240,16 +1443,25 @@ __device__ __forceinline__ void norm_final_block(const DevView& d, double* sh) {
   }
 }
 
-// the block's sum of d2 into partials[blockIdx.x]; the block that finishes
-// last (d.nblk_red == gridDim.x) reduces all partials into the step's norms;
-// sh: 4 x 256 doubles of shared memory
-__device__ __forceinline__ void stage_norms(const DevView& d, const double* d2, double* sh) {
+// the block's sum of na into partials[blockIdx.x] (mixed precision and
+// double-float: four FP32 pairs in the same 32 bytes); the block that finishes last
+// (d.nblk_red == gridDim.x) reduces all partials into the step's norms;
+// sh: FVS_NORM_SH_BYTES of shared memory
+__device__ __forceinline__ void stage_norms(const DevView& d, NormAcc& na, void* sh) {
   __shared__ int s_last;
+#if FVS_MIXED || FVS_DF
+  block_pairs4(na, static_cast<float2*>(sh));
+  if (threadIdx.x == 0) {
+    float2* P = reinterpret_cast<float2*>(d.partials) + 4 * (size_t)blockIdx.x;
+#pragma unroll
+    for (int k = 0; k < 4; k++) P[k] = make_float2(na.h[k], na.l[k]);
+#else
   double out[4];
-  block_sum4_in(d2, out, sh);
+  block_sum4_in(na.s, out, static_cast<double*>(sh));
   if (threadIdx.x == 0) {
 #pragma unroll
     for (int k = 0; k < 4; k++) d.partials[4 * blockIdx.x + k] = out[k];
+#endif
     __threadfence();
     s_last = atomicAdd(&d.stepctl[1], 1) == (int)gridDim.x - 1;
   }
@@ -1264,15 +1476,22 @@ __device__ __forceinline__ void stage_norms(const DevView& d, const double* d2, 
 // One RK stage over all cells.  At the last stage every block writes its
 // partial norms; the block that finishes last (a counter in stepctl[1])
 // reduces them, so no separate norm launch is needed.
-template <int MODE>
+// STRIDE: one wave of resident blocks strides over the cells (the last
+// stage's launch); otherwise one cell per thread.
+template <int MODE, bool STRIDE>
 __global__ void __launch_bounds__(256) k_update(const DevView d, const StageParams sp) {
   pdl_wait();
   pdl_trigger();
-  const int ic = blockIdx.x * blockDim.x + threadIdx.x;
-  double d2[4] = {0.0, 0.0, 0.0, 0.0};
-  if (ic < d.nc) update_item<MODE, false>(d, sp, ic, d2);
-  __shared__ double sh[4 * 256];
-  if (sp.last) stage_norms(d, d2, sh);
+  NormAcc na;
+  if (STRIDE) {
+    for (int ic = blockIdx.x * blockDim.x + threadIdx.x; ic < d.nc; ic += gridDim.x * blockDim.x)
+      update_item<MODE, false>(d, sp, ic, na);
+  } else {
+    const int ic = blockIdx.x * blockDim.x + threadIdx.x;
+    if (ic < d.nc) update_item<MODE, false>(d, sp, ic, na);
+  }
+  __shared__ __align__(16) unsigned char sh[FVS_NORM_SH_BYTES];
+  if (sp.last) stage_norms(d, na, sh);
 }
 
 #if FVS_MIXED || FVS_DF
@@ -1389,7 +1608,7 @@ __global__ void __launch_bounds__(256, FVS_MIXED ? 5 : 2) k_tile_stage(const Dev
   }
   __syncthreads();
   // 4. gather and RK update of the tile's cells
-  double d2[4] = {0.0, 0.0, 0.0, 0.0};
+  NormAcc na;
   const bool want_ws = sp.steady && sp.stage == 1;
   for (int i = tid; i < n; i += nthr) {
     const int gid = b + i;
@@ -1404,18 +1623,19 @@ __global__ void __launch_bounds__(256, FVS_MIXED ? 5 : 2) k_tile_stage(const Dev
 #if FVS_MIXED
     float res[4], ws;
     residual_from_faces_f(sl, -static_cast<const float*>(d.volT)[gid], want_ws, get, res, ws);
-    apply_stage_f<MODE, false>(d, sp, gid, res, ws, Pout, d2);
+    apply_stage_f<MODE, false>(d, sp, gid, res, ws, Pout, na);
 #else
-    double res[4], ws;
+    df64 res[4];
+    double ws;
     const df64 rv = -static_cast<const df64*>(d.volT)[gid];
     if (want_ws) residual_from_faces_df<true>(sl, rv, get, res, ws);
     else residual_from_faces_df<false>(sl, rv, get, res, ws);
-    apply_stage_d<MODE, false>(d, sp, gid, res, ws, Pout, d2);
+    apply_stage_df<MODE, false>(d, sp, gid, res, ws, Pout, na);
 #endif
   }
   // the norm reduction reuses the primitives' shared memory, unused in
   // phase 4 (at least 4 x 256 doubles: tile_smem_bytes)
-  if (sp.last) stage_norms(d, d2, reinterpret_cast<double*>(tile_shm));
+  if (sp.last) stage_norms(d, na, tile_shm);
 }
 
 template <int MODE, int REC, int LIM>
@@ -1479,7 +1699,7 @@ __global__ void __launch_bounds__(256) k_tile_flux_update(const DevView d, const
     sF[5 * f + 4] = wsa;
   }
   __syncthreads();
-  double d2[4] = {0.0, 0.0, 0.0, 0.0};
+  NormAcc na;
   const bool want_ws = sp.steady && sp.stage == 1;
   for (int i = tid; i < n; i += nthr) {
     const int gid = b + i;
@@ -1494,18 +1714,19 @@ __global__ void __launch_bounds__(256) k_tile_flux_update(const DevView d, const
 #if FVS_MIXED
     float res[4], ws;
     residual_from_faces_f(sl, -static_cast<const float*>(d.volT)[gid], want_ws, get, res, ws);
-    apply_stage_f<MODE, false>(d, sp, gid, res, ws, Pout, d2);
+    apply_stage_f<MODE, false>(d, sp, gid, res, ws, Pout, na);
 #else
-    double res[4], ws;
+    df64 res[4];
+    double ws;
     const df64 rv = -static_cast<const df64*>(d.volT)[gid];
     if (want_ws) residual_from_faces_df<true>(sl, rv, get, res, ws);
     else residual_from_faces_df<false>(sl, rv, get, res, ws);
-    apply_stage_d<MODE, false>(d, sp, gid, res, ws, Pout, d2);
+    apply_stage_df<MODE, false>(d, sp, gid, res, ws, Pout, na);
 #endif
   }
   if (sp.last) {
     __syncthreads();  // the norm buffer reuses the flux records
-    stage_norms(d, d2, reinterpret_cast<double*>(tile_shm));
+    stage_norms(d, na, tile_shm);
   }
 }
 
@@ -1669,7 +1890,7 @@ __global__ void __launch_bounds__(256) k_tile_dma(const DevView d, const TileVie
   // 4. gather, RK update, new primitives to every record of the cell
   float* GBo = static_cast<float*>(dv.GB[kout]);
   float* Pv = static_cast<float*>(d.Pv);
-  double d2[4] = {0.0, 0.0, 0.0, 0.0};
+  NormAcc na;
   const bool want_ws = sp.steady && sp.stage == 1;
   for (int i = tid; i < n; i += nthr) {
     const int gid = b + i;
@@ -1687,11 +1908,11 @@ __global__ void __launch_bounds__(256) k_tile_dma(const DevView d, const TileVie
     apply_stage_fs<MODE, false>(d, sp, gid, res, ws, [&](const float* p) {
       for (int j = j0; j < j1; j++) st4(GBo, dv.dpos[j], p);
       if (sp.last) st4(Pv, gid, p);
-    }, d2);
+    }, na);
   }
   if (sp.last) {
     __syncthreads();  // the norm buffer reuses the gradient regions
-    stage_norms(d, d2, reinterpret_cast<double*>(dsm + dv.o_Gx));
+    stage_norms(d, na, dsm + dv.o_Gx);
   }
 }
 
@@ -1869,10 +2090,11 @@ __device__ __forceinline__ bool grid_sync(GridBarrier* gb, long long budget) {
 template <int MODE>
 __device__ __forceinline__ void update_tile(const DevView& d, const PersistPlan& p, const StageParams& sp, int t) {
   const int4 tl = p.cell_tiles[t];
-  double d2[4] = {0.0, 0.0, 0.0, 0.0};
-  for (int ic = tl.x + threadIdx.x; ic < tl.y; ic += blockDim.x) update_item<MODE, true>(d, sp, ic, d2);
+  NormAcc na;
+  for (int ic = tl.x + threadIdx.x; ic < tl.y; ic += blockDim.x) update_item<MODE, true>(d, sp, ic, na);
   if (sp.last) {
-    double out[4];
+    double d2[4], out[4];
+    na.to_double(d2);
     block_sum4(d2, out);
     if (threadIdx.x == 0)
 #pragma unroll
@@ -1993,7 +2215,7 @@ __device__ __forceinline__ void face_flux_first(const DevView& d, const float* p
 // sign.
 template <int MODE>
 __device__ __forceinline__ void cell_stage_item(const DevView& d, const StageParams& sp, const float* Pin,
-                                                float* Pout, int ic, double time, double* d2) {
+                                                float* Pout, int ic, double time, NormAcc& na) {
   const int4 cf = d.cflist[ic];
   FaceRec f0, f1, f2, f3;
   load_face(d, Pin, cf.x, f0);
@@ -2022,17 +2244,18 @@ __device__ __forceinline__ void cell_stage_item(const DevView& d, const StagePar
   float res[4];
 #pragma unroll
   for (int v = 0; v < 4; v++) res[v] = (hi[v] + lo[v]) * rv;
-  apply_stage_f<MODE, true>(d, sp, ic, res, wh + wl, Pout, d2);
+  apply_stage_f<MODE, true>(d, sp, ic, res, wh + wl, Pout, na);
 }
 
 template <int MODE>
 __device__ __forceinline__ void cell_stage_tile(const DevView& d, const PersistPlan& p, const StageParams& sp,
                                                 const float* Pin, float* Pout, int t, double time) {
   const int4 tl = p.cell_tiles[t];
-  double d2[4] = {0.0, 0.0, 0.0, 0.0};
-  for (int ic = tl.x + threadIdx.x; ic < tl.y; ic += blockDim.x) cell_stage_item<MODE>(d, sp, Pin, Pout, ic, time, d2);
+  NormAcc na;
+  for (int ic = tl.x + threadIdx.x; ic < tl.y; ic += blockDim.x) cell_stage_item<MODE>(d, sp, Pin, Pout, ic, time, na);
   if (sp.last) {
-    double out[4];
+    double d2[4], out[4];
+    na.to_double(d2);
     block_sum4(d2, out);
     if (threadIdx.x == 0)
 #pragma unroll
@@ -2251,12 +2474,44 @@ static void launch_flux(const DevView& d, double dts, cudaStream_t s) {
   else launch_k(k_flux<REC_GENERAL>, grid_of(d.nedge), 256, 0, s, d, dts);
 }
 
-static void launch_update(const DevView& d, const StageParams& sp, cudaStream_t s) {
+// blocks of 256 threads of kernel k resident on the whole device at once
+template <class K>
+static unsigned resident_blocks(K k) {
+  int dev = 0, nsm = 0, per_sm = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, 256, 0) != cudaSuccess || nsm <= 0 || per_sm <= 0)
+    return 0;
+  return (unsigned)(nsm * per_sm);
+}
+
+static int update_wave(int mode) {
+  const unsigned w = mode == MODE_SSP42 ? resident_blocks(k_update<MODE_SSP42, true>)
+                     : mode == MODE_SSP3 ? resident_blocks(k_update<MODE_SSP3, true>)
+                                         : resident_blocks(k_update<MODE_RK, true>);
+  return (int)w;
+}
+
+template <int MODE>
+static void launch_update_mode(const DevView& d, const StageParams& sp, cudaStream_t s) {
   const unsigned g = grid_of(d.nc);
+  if (!sp.last || d.upd_grid <= 0 || (unsigned)d.upd_grid >= g) {
+    launch_k(k_update<MODE, false>, g, 256, 0, s, d, sp);
+    return;
+  }
+  // The last stage reduces the norms: one wave of resident blocks walks the
+  // cells (grid stride), so that the block-end reduction, fence and counter
+  // run once per resident block instead of once per 256 cells, and the last
+  // block sums that many partials.
+  DevView dl = d;
+  dl.nblk_red = d.upd_grid;
+  launch_k(k_update<MODE, true>, (unsigned)d.upd_grid, 256, 0, s, dl, sp);
+}
+
+static void launch_update(const DevView& d, const StageParams& sp, cudaStream_t s) {
   switch (sp.mode) {
-    case MODE_SSP42: launch_k(k_update<MODE_SSP42>, g, 256, 0, s, d, sp); break;
-    case MODE_SSP3: launch_k(k_update<MODE_SSP3>, g, 256, 0, s, d, sp); break;
-    default: launch_k(k_update<MODE_RK>, g, 256, 0, s, d, sp); break;
+    case MODE_SSP42: launch_update_mode<MODE_SSP42>(d, sp, s); break;
+    case MODE_SSP3: launch_update_mode<MODE_SSP3>(d, sp, s); break;
+    default: launch_update_mode<MODE_RK>(d, sp, s); break;
   }
 }
 
