@@ -228,27 +228,30 @@ def fp64_pipe_frac(kernel: str):
 
 
 def algorithmic_bytes(kernel: str, ncells: int, nedges: int, tsize: int) -> float:
-    """Compulsory bytes of one launch (every array read or written once).
+    """Compulsory bytes of one launch (every array read or written once) on
+    the bench's unsteady workload, where no kernel reads or writes the
+    wave-speed records (only a steady scheme's first stage needs them).
 
     gradient (LSQ-fn, tri): per cell own primitives 4T, stencil ptr 4 +
-      3 ids 12 + 3 coef 6T + 3 weights 3T, gradient out 8T.
+      3 ids 12 + 3 coefficients 6T (the LSQ weights are folded into them;
+      the strict build reads 3T more), gradient out 8T.
     flux: per edge ids 8 + normal 2T + area T + two offsets 4T, flux*area out
-      4T + ws out T; per cell primitives, gradient and limiter 13T.
+      4T; per cell primitives, gradient and limiter 13T.
     update: per cell gather list 16 + vol 8 + U 32 read + U0 32 + U 32 write
-      + primitives out 4T; per edge flux slot 5T read once.  Mixed (T = 4):
+      + primitives out 4T; per edge flux slot 4T read once.  Mixed (T = 4):
       gather list 16 + 1/vol 4 + primitives out 16, and the state as the
       mixed update moves it in an SSP-RK3 step: U read at every stage, the
       FP32 increment written at stages 1-2 and read at 2-3, U written at
       stage 3, i.e. (48 + 64 + 80) / 3 = 64 B per stage."""
     T = tsize
     if kernel == "gradient":
-        return ncells * (4 * T + 16 + 6 * T + 3 * T + 8 * T)
+        return ncells * (4 * T + 16 + 6 * T + 8 * T)
     if kernel == "flux":
-        return nedges * (8 + 7 * T + 5 * T) + ncells * 13 * T
+        return nedges * (8 + 7 * T + 4 * T) + ncells * 13 * T
     if kernel == "update":
         if T == 4:
-            return ncells * (16 + 4 + 64 + 4 * T) + nedges * 5 * T
-        return ncells * (16 + 8 + 32 + 32 + 32 + 4 * T) + nedges * 5 * T
+            return ncells * (16 + 4 + 64 + 4 * T) + nedges * 4 * T
+        return ncells * (16 + 8 + 32 + 32 + 32 + 4 * T) + nedges * 4 * T
     return 0.0
 
 

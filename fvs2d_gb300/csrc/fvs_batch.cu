@@ -986,7 +986,7 @@ int fvs_batch_run_to_level_dc(fvs_batch* b, int32_t max_steps, const double* lev
     // base state of the chunk: fold, FP64 residual and wave speeds, FP32 copies
     K.fold(*d32, b->dc, d64.U, b->stream);
     K64.cvar2pvar(d64, b->stream);
-    K64.flux(d64, 0.0, b->stream);
+    K64.flux(d64, 0.0, true, b->stream);
     K64.residual_out(d64, b->stream);
     K.base(*d32, b->dc, d64.U, d64.resid, d64.ws, b->stream);
     *b->h_step0 = step;

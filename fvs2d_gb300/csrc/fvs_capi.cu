@@ -411,7 +411,7 @@ void enqueue_step(fvs_handle* H) {
   }
   for (const StageParams& sp : H->stages) {
     K.gradient(H->d, s);
-    K.flux(H->d, sp.dts, s);
+    K.flux(H->d, sp.dts, sp.steady && sp.stage == 1, s);
     K.update(H->d, sp, s);
   }
 }
@@ -468,7 +468,7 @@ int device_residual(fvs_handle* H, double time) {
   if (e != cudaSuccess) return H->cuda_fail(e, "time upload");
   H->ks->cvar2pvar(H->d, H->stream);
   H->ks->gradient(H->d, H->stream);
-  H->ks->flux(H->d, 0.0, H->stream);
+  H->ks->flux(H->d, 0.0, true, H->stream);
   H->ks->residual_out(H->d, H->stream);
   return check_launch(H, "residual kernels");
 }
@@ -1033,7 +1033,7 @@ int fvs_profile_step(fvs_handle* h, int32_t cap, int32_t* n, char* names, float*
     for (const StageParams& sp : h->stages) {
       K.gradient(h->d, s);
       mark("gradient");
-      K.flux(h->d, sp.dts, s);
+      K.flux(h->d, sp.dts, sp.steady && sp.stage == 1, s);
       mark("flux");
       K.update(h->d, sp, s);
       mark("update");

@@ -277,7 +277,9 @@ struct KernelSet {
   void (*begin_step)(const DevView&, cudaStream_t);
   void (*cvar2pvar)(const DevView&, cudaStream_t);
   void (*gradient)(const DevView&, cudaStream_t);
-  void (*flux)(const DevView&, double dts, cudaStream_t);
+  // ws_out: also store the wave-speed records (a steady scheme's first stage
+  // and residual evaluations read them)
+  void (*flux)(const DevView&, double dts, bool ws_out, cudaStream_t);
   void (*update)(const DevView&, const StageParams&, cudaStream_t);
   void (*residual_out)(const DevView&, cudaStream_t);
   // persistent kernel (LSQ gradients): resident blocks per SM for a block

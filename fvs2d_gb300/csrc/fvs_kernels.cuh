@@ -780,12 +780,14 @@ __device__ __forceinline__ void flux_compute(const DevView& d, int e, double tim
   flux_eval(d, pfL, pfR, n, af, flux, wsa);
 }
 
+// ws_out: also store ws * area (read only by a steady scheme's first stage,
+// for the local time step, and by residual evaluations)
 template <int REC, bool COH>
-__device__ __forceinline__ void flux_item(const DevView& d, int e, double time) {
+__device__ __forceinline__ void flux_item(const DevView& d, int e, double time, bool ws_out = true) {
   T flux[4], wsa;
   flux_compute<REC, COH>(d, e, time, flux, wsa);
   st4(static_cast<T*>(d.eflux), e, flux);
-  static_cast<T*>(d.ews)[e] = wsa;
+  if (ws_out) static_cast<T*>(d.ews)[e] = wsa;
 }
 
 // First-order flux of two edge slots per call (e1 < 0: e0 alone).  The
@@ -833,11 +835,11 @@ __device__ __forceinline__ void flux_range(const DevView& d, int b, int end, int
 }
 
 template <int REC>
-__global__ void __launch_bounds__(256) k_flux(const DevView d, double dts) {
+__global__ void __launch_bounds__(256) k_flux(const DevView d, double dts, int ws_out) {
   pdl_wait();
   pdl_trigger();
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
-  if (e < d.nedge) flux_item<REC, false>(d, e, d.tctl[1] + dts);
+  if (e < d.nedge) flux_item<REC, false>(d, e, d.tctl[1] + dts, ws_out != 0);
 }
 
 // ---------------------------------------------------------------------------
@@ -936,15 +938,40 @@ __device__ __forceinline__ void gather_slot(const DevView& d, int s, double* r, 
   if (WS) ws = ws + ldc1<COH>(static_cast<const double*>(d.ews), idx);
 }
 
+// the flux slots of cell ic summed in its gather order (the reference's
+// order); the FP64 build starts the sums from the first slot instead of from
+// zero (the same values, four additions fewer)
 template <bool WS, bool COH>
-__device__ __forceinline__ void cell_residual(const DevView& d, int ic, double* res, double& ws) {
-  double r[4] = {0.0, 0.0, 0.0, 0.0};
+__device__ __forceinline__ void cell_flux_sum(const DevView& d, int ic, double* r, double& ws) {
   ws = 0.0;
   const int4 cf = d.cflist[ic];
+#if FVS_STRICT
+#pragma unroll
+  for (int v = 0; v < 4; v++) r[v] = 0.0;
   gather_slot<WS, COH>(d, cf.x, r, ws);
+#else
+  if (cf.x != 0) {
+    const int idx = chk_idx(d.bounds_err, (cf.x > 0 ? cf.x : -cf.x) - 1, 0, d.nedge, SITE_GATHER);
+    ldc4<COH>(static_cast<const double*>(d.eflux), idx, r);
+    if (cf.x < 0) {
+#pragma unroll
+      for (int v = 0; v < 4; v++) r[v] = -r[v];
+    }
+    if (WS) ws = ldc1<COH>(static_cast<const double*>(d.ews), idx);
+  } else {
+#pragma unroll
+    for (int v = 0; v < 4; v++) r[v] = 0.0;
+  }
+#endif
   gather_slot<WS, COH>(d, cf.y, r, ws);
   gather_slot<WS, COH>(d, cf.z, r, ws);
   gather_slot<WS, COH>(d, cf.w, r, ws);
+}
+
+template <bool WS, bool COH>
+__device__ __forceinline__ void cell_residual(const DevView& d, int ic, double* res, double& ws) {
+  double r[4];
+  cell_flux_sum<WS, COH>(d, ic, r, ws);
 #if FVS_STRICT
   const double vol = d.vol[ic];
 #pragma unroll
@@ -1229,9 +1256,15 @@ __device__ __forceinline__ void update_item(const DevView& d, const StageParams&
 // the RK stage of one cell from its residual res (and, at a steady first
 // stage, its wave-speed sum ws); the new primitives go to Pout; at the last
 // stage adds |U-U0|^2 to na
-template <int MODE, bool COH>
-__device__ __forceinline__ void apply_stage_d(const DevView& d, const StageParams& sp, int ic, const double* res,
-                                              double ws, T* Pout, NormAcc& na) {
+// RAW (FP64 build): res holds the flux sums and rv = -1/vol; SSP-RK3 folds
+// rv into the step (h rv, one product per cell instead of four), the other
+// schemes scale res first.
+template <int MODE, bool COH, bool RAW = false>
+__device__ __forceinline__ void apply_stage_d(const DevView& d, const StageParams& sp, int ic, const double* res_in,
+                                              double ws, T* Pout, NormAcc& na, double rv = 1.0) {
+  double res[4];
+#pragma unroll
+  for (int v = 0; v < 4; v++) res[v] = (RAW && MODE != MODE_SSP3) ? res_in[v] * rv : res_in[v];
   {
     double h = sp.h;
     if (sp.steady) {
@@ -1279,9 +1312,10 @@ __device__ __forceinline__ void apply_stage_d(const DevView& d, const StageParam
       } else {
         ldc4<COH>(d.U, ic, cur);
       }
+      const double hs = RAW ? h * rv : h;
 #pragma unroll
       for (int v = 0; v < 4; v++) {
-        const double s = cur[v] + h * res[v];
+        const double s = cur[v] + hs * res[v];
         u[v] = sp.stage == 1 ? s : sp.a * u0[v] + sp.b * s;
       }
     }
@@ -1402,9 +1436,15 @@ __device__ __forceinline__ void update_item(const DevView& d, const StageParams&
 template <int MODE, bool COH>
 __device__ __forceinline__ void update_item(const DevView& d, const StageParams& sp, int ic, NormAcc& na) {
   double res[4], ws;
+#if FVS_STRICT
   if (sp.steady && sp.stage == 1) cell_residual<true, COH>(d, ic, res, ws);
   else cell_residual<false, COH>(d, ic, res, ws);
   apply_stage_d<MODE, COH>(d, sp, ic, res, ws, static_cast<T*>(d.Pv), na);
+#else
+  if (sp.steady && sp.stage == 1) cell_flux_sum<true, COH>(d, ic, res, ws);
+  else cell_flux_sum<false, COH>(d, ic, res, ws);
+  apply_stage_d<MODE, COH, true>(d, sp, ic, res, ws, static_cast<T*>(d.Pv), na, -d.rvol[ic]);
+#endif
 }
 #endif
 
@@ -2467,11 +2507,12 @@ static void launch_gradient(const DevView& d, cudaStream_t s) {
   }
 }
 
-static void launch_flux(const DevView& d, double dts, cudaStream_t s) {
+static void launch_flux(const DevView& d, double dts, bool ws_out, cudaStream_t s) {
   const bool spec = !FVS_STRICT && d.khalf == 0.0 && d.omk == 1.0 && d.limiter == FVS_LIM_NONE && !d.first_order;
-  if (d.first_order) launch_k(k_flux<REC_FIRST>, grid_of(d.nedge), 256, 0, s, d, dts);
-  else if (spec) launch_k(k_flux<REC_SPEC>, grid_of(d.nedge), 256, 0, s, d, dts);
-  else launch_k(k_flux<REC_GENERAL>, grid_of(d.nedge), 256, 0, s, d, dts);
+  const int w = ws_out ? 1 : 0;
+  if (d.first_order) launch_k(k_flux<REC_FIRST>, grid_of(d.nedge), 256, 0, s, d, dts, w);
+  else if (spec) launch_k(k_flux<REC_SPEC>, grid_of(d.nedge), 256, 0, s, d, dts, w);
+  else launch_k(k_flux<REC_GENERAL>, grid_of(d.nedge), 256, 0, s, d, dts, w);
 }
 
 // blocks of 256 threads of kernel k resident on the whole device at once
