@@ -338,7 +338,8 @@ def run_ours(args) -> dict:
     launches = s.launches_per_step() * args.steps
     out = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
            "ms_per_step": t * 1e3 / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-           "dtype": "f64" if prec != PREC_MIXED else "f32 flux/gradient, f64 accumulation/update",
+           "dtype": {PREC_MIXED: "f32 flux/gradient/increment, f64 state",
+                     PREC_FP64_DF: "df64 (FP32 pairs) arithmetic, f64 state"}.get(prec, "f64"),
            "data": "synthetic (seeded mesh generator, analytic vortex initial state)",
            "config": config_dict(nc, nst, args.precision), "e2e": e2e, "roofline": roofline, "clocks": clocks,
            "gpu_launches": launches}

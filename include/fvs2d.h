@@ -71,16 +71,19 @@ extern "C" {
  * FP64:        same operations, FMA contraction allowed, reciprocals and
  *              square roots from the hardware approximations refined by a
  *              Newton-Raphson step (fast FP64 drop-in).
- * MIXED:       gradients, limiter, reconstruction and flux in FP32; residual
- *              accumulation, state update and norms in FP64.  The LSQ weight
- *              matrices are built in FP64 and rounded once to FP32 for the
- *              gradient: that rounding moves the gradient by at most 8.8e-8
- *              of max|grad| (1,048,576-cell vortex), against 1.3e-5 from the
- *              FP32 primitives the weights multiply.
- * FP64_DF:     gradients, limiter, reconstruction, flux and the residual
- *              gather in double-float (pairs of FP32, 48-bit significand:
- *              FP64-class accuracy on the FP32 pipe); FP64 state update,
- *              local time step and norms.                                   */
+ * MIXED:       gradients, limiter, reconstruction and flux in FP32; the
+ *              residual accumulated exactly (TwoSum), the RK increment in
+ *              FP32 added to the FP64 state, which is stored in FP64; norms
+ *              summed as pairs of FP32 numbers (~48 significant bits).  The
+ *              LSQ weight matrices are built in FP64 and rounded once to FP32
+ *              for the gradient: that rounding moves the gradient by at most
+ *              8.8e-8 of max|grad| (1,048,576-cell vortex), against 1.3e-5
+ *              from the FP32 primitives the weights multiply.
+ * FP64_DF:     gradients, limiter, reconstruction, flux, the residual gather
+ *              and the RK stage in double-float (pairs of FP32, 48-bit
+ *              significand: FP64-class accuracy on the FP32 pipe); the state
+ *              is stored in FP64 (exactly its double-float value), the local
+ *              time step is FP64, the norms are summed as FP32 pairs.       */
 #define FVS_PREC_FP64_STRICT 0
 #define FVS_PREC_FP64        1
 #define FVS_PREC_MIXED       2

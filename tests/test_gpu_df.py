@@ -1,8 +1,9 @@
 """Double-float path (FVS_PREC_FP64_DF) vs the CPU oracle.
 
-Gradient, limiter, reconstruction, Roe flux and the residual gather run in
-pairs of FP32 numbers (48-bit significand, relative precision 2^-48 per
-operation against FP64's 2^-53); the state update and the norms are FP64.
+Gradient, limiter, reconstruction, Roe flux, the residual gather and the RK
+stage run in pairs of FP32 numbers (48-bit significand, relative precision
+2^-48 per operation against FP64's 2^-53); the state is stored in FP64 and
+the norms are summed as FP32 pairs.
 The bar is the FP64 drop-in's: max|diff| <= 1e-12 * max|ref| per residual,
 gradient and step; the limiter value itself is held to 1e-11.
 """
