@@ -141,7 +141,7 @@ struct DevView {
   float fgamma = 1.4f, fgm1 = 0.4f, figm1 = 2.5f, fkhalf = 0, fnkhalf = 0, fomk = 1;
   // and split into FP32 pairs (hi, lo) for the double-float kernels
   float dgamma[2] = {1.4f, 0}, dgm1[2] = {0.4f, 0}, digm1[2] = {2.5f, 0}, dkhalf[2] = {0, 0}, dnkhalf[2] = {0, 0},
-        domk[2] = {1, 0};
+        domk[2] = {1, 0}, dggm1[2] = {3.5f, 0};
   const void* volT = nullptr;    // [nc] 1/vol in the compute type (GG gradients)
   int limiter = 0, grad_method = 3, first_order = 0, vortex = 0;
   double vx = 0, vy = 0, vkappa = 0, vinf[4] = {0, 0, 0, 0};
@@ -158,7 +158,7 @@ inline void set_fp32_constants(DevView& d) {
   d.fgamma = float(d.gamma); d.fgm1 = float(d.gm1); d.figm1 = float(d.igm1);
   d.fkhalf = float(d.khalf); d.fnkhalf = float(d.nkhalf); d.fomk = float(d.omk);
   split(d.gamma, d.dgamma); split(d.gm1, d.dgm1); split(d.igm1, d.digm1);
-  split(d.khalf, d.dkhalf); split(d.nkhalf, d.dnkhalf); split(d.omk, d.domk);
+  split(d.khalf, d.dkhalf); split(d.nkhalf, d.dnkhalf); split(d.omk, d.domk); split(d.ggm1, d.dggm1);
 }
 
 // Device view of a TilePlan (fvs_tiles.hpp) for the fused RK stage: one
