@@ -9,6 +9,8 @@ one step must equal sqrt(mean((U1 - U0)^2)) of the downloaded states: every
 cell counted once.  The states are FP64 in every mode; the mixed increment is
 an FP32 number added to the FP64 state, so its norm agrees to the FP32
 rounding of the squares."""
+import math
+
 import numpy as np
 import pytest
 
@@ -33,8 +35,13 @@ def test_one_wave_norm_counts_every_cell_once(prec):
         s.cvar = u0
         s.time_integration(0.0, 1)
         u1 = s.cvar
-    ref1 = np.sqrt(((u1 - u0) ** 2).mean(0))
-    ref2 = np.sqrt(((u2 - u1) ** 2).mean(0))
+    # exactly rounded sums (numpy's sum along the long axis is sequential,
+    # ~1e-13 relative at this size)
+    def rms(a, b):
+        d2 = (a - b) ** 2
+        return np.array([math.sqrt(math.fsum(d2[:, k]) / d2.shape[0]) for k in range(4)])
+
+    ref1, ref2 = rms(u1, u0), rms(u2, u1)
     assert np.all(ref1 > 0) and np.all(ref2 > 0)
     assert np.allclose(norms[0], ref1, rtol=TOL[prec], atol=0), (norms[0], ref1)
     assert np.allclose(norms[1], ref2, rtol=TOL[prec], atol=0), (norms[1], ref2)
