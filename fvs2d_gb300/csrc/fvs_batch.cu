@@ -326,6 +326,7 @@ int build_plan(fvs_batch* B) {
   if (e == cudaSuccess && !cases.empty()) e = cudaMemcpy(B->d_case_tiles, cases.data(), 16 * cases.size(), cudaMemcpyHostToDevice);
   if (e != cudaSuccess) return B->cuda_fail(e, "plan upload");
   PersistPlan& P = B->plan;
+  P.tile = B->tile;
   P.nstages = (int)B->stages.size();
   for (int k = 0; k < P.nstages; k++) P.sp[k] = B->stages[k];
   P.t1 = 0.0;

@@ -261,6 +261,7 @@ struct PersistPlan {
   int ncell_tiles = 0;
   const int2* edge_tiles = nullptr;      // x = first edge slot, y = end
   int nedge_tiles = 0;
+  int tile = 0;                          // tile length (cells or edge slots)
   const int4* case_tiles = nullptr;      // x = case, y = first cell tile, z = end tile, w = cells of the case
   int ncase_active = 0;
   double* tile_partials = nullptr;       // [ncell_tiles][4]

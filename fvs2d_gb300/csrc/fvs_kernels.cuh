@@ -2503,16 +2503,32 @@ __global__ void __launch_bounds__(256) k_tiles_gradient(const DevView d, const P
   for (int ic = tl.x + threadIdx.x; ic < tl.y; ic += blockDim.x) gradient_item<FVS_GRAD_LSQ, LIM, false>(d, ic);
 }
 
-template <int REC>
+// ONE: tiles as long as the block, one edge slot or cell per thread (the
+// single-mesh kernels' shape and register budget: no paired slots, no loop)
+template <int REC, bool ONE>
 __global__ void __launch_bounds__(256) k_tiles_flux(const DevView d, const PersistPlan p, int stage) {
   const double told = p.t1 + double(*p.step0_dev) * d.dt;
   const int2 tl = p.edge_tiles[blockIdx.x];
-  flux_range<REC, false>(d, tl.x + threadIdx.x, tl.y, blockDim.x, told + p.sp[stage].dts);
+  if (ONE) {
+    const int e = tl.x + threadIdx.x;
+    if (e < tl.y) flux_item<REC, false>(d, e, told + p.sp[stage].dts);
+  } else {
+    flux_range<REC, false>(d, tl.x + threadIdx.x, tl.y, blockDim.x, told + p.sp[stage].dts);
+  }
 }
 
-template <int MODE>
+template <int MODE, bool ONE>
 __global__ void __launch_bounds__(256) k_tiles_update(const DevView d, const PersistPlan p, int stage) {
-  update_tile<MODE>(d, p, p.sp[stage], blockIdx.x);
+  if (ONE) {
+    const StageParams& sp = p.sp[stage];
+    const int4 tl = p.cell_tiles[blockIdx.x];
+    const int ic = tl.x + threadIdx.x;
+    NormAcc na;
+    if (ic < tl.y) update_item<MODE, false>(d, sp, ic, na);
+    if (sp.last) tile_norm_partial(p, na, blockIdx.x);
+  } else {
+    update_tile<MODE>(d, p, p.sp[stage], blockIdx.x);
+  }
 }
 
 // per-case RMS of the step from the tile partials (fixed order), one block
@@ -2538,6 +2554,7 @@ __global__ void __launch_bounds__(256) k_tiles_norms(const PersistPlan p) {
 }
 
 static cudaError_t launch_tiled_step(const DevView& d, const PersistPlan& p, int block, cudaStream_t s) {
+  const bool one = p.tile == block;
 #if FVS_MIXED
   if (cell_fused(d)) {
     for (int k = 0; k < p.nstages; k++) {
@@ -2556,13 +2573,24 @@ static cudaError_t launch_tiled_step(const DevView& d, const PersistPlan& p, int
       if (d.limiter != FVS_LIM_NONE) k_tiles_gradient<1><<<p.ncell_tiles, block, 0, s>>>(d, p);
       else k_tiles_gradient<0><<<p.ncell_tiles, block, 0, s>>>(d, p);
     }
-    if (d.first_order) k_tiles_flux<REC_FIRST><<<p.nedge_tiles, block, 0, s>>>(d, p, k);
-    else if (persistent_spec(d)) k_tiles_flux<REC_SPEC><<<p.nedge_tiles, block, 0, s>>>(d, p, k);
-    else k_tiles_flux<REC_GENERAL><<<p.nedge_tiles, block, 0, s>>>(d, p, k);
+    if (one) {
+      if (d.first_order) k_tiles_flux<REC_FIRST, true><<<p.nedge_tiles, block, 0, s>>>(d, p, k);
+      else if (persistent_spec(d)) k_tiles_flux<REC_SPEC, true><<<p.nedge_tiles, block, 0, s>>>(d, p, k);
+      else k_tiles_flux<REC_GENERAL, true><<<p.nedge_tiles, block, 0, s>>>(d, p, k);
+      switch (p.sp[k].mode) {
+        case MODE_SSP42: k_tiles_update<MODE_SSP42, true><<<p.ncell_tiles, block, 0, s>>>(d, p, k); break;
+        case MODE_SSP3: k_tiles_update<MODE_SSP3, true><<<p.ncell_tiles, block, 0, s>>>(d, p, k); break;
+        default: k_tiles_update<MODE_RK, true><<<p.ncell_tiles, block, 0, s>>>(d, p, k); break;
+      }
+      continue;
+    }
+    if (d.first_order) k_tiles_flux<REC_FIRST, false><<<p.nedge_tiles, block, 0, s>>>(d, p, k);
+    else if (persistent_spec(d)) k_tiles_flux<REC_SPEC, false><<<p.nedge_tiles, block, 0, s>>>(d, p, k);
+    else k_tiles_flux<REC_GENERAL, false><<<p.nedge_tiles, block, 0, s>>>(d, p, k);
     switch (p.sp[k].mode) {
-      case MODE_SSP42: k_tiles_update<MODE_SSP42><<<p.ncell_tiles, block, 0, s>>>(d, p, k); break;
-      case MODE_SSP3: k_tiles_update<MODE_SSP3><<<p.ncell_tiles, block, 0, s>>>(d, p, k); break;
-      default: k_tiles_update<MODE_RK><<<p.ncell_tiles, block, 0, s>>>(d, p, k); break;
+      case MODE_SSP42: k_tiles_update<MODE_SSP42, false><<<p.ncell_tiles, block, 0, s>>>(d, p, k); break;
+      case MODE_SSP3: k_tiles_update<MODE_SSP3, false><<<p.ncell_tiles, block, 0, s>>>(d, p, k); break;
+      default: k_tiles_update<MODE_RK, false><<<p.ncell_tiles, block, 0, s>>>(d, p, k); break;
     }
   }
   k_tiles_norms<<<p.ncase_active, block, 0, s>>>(p);
