@@ -443,12 +443,14 @@ class ShapeTrials {
     const LaunchShape cur = {b->tiled, b->fuse, b->block, b->tile, b->bps};
     cand_.push_back(cur);
     // separate phases: large tiles at high occupancy suit large active sets,
-    // short tiles and few blocks small ones
+    // short tiles and few blocks small ones; tiles as long as the block run
+    // one item per thread (the single-mesh kernels' shape)
     const bool sep = dc ? b->fuse : false;
     for (const LaunchShape& s : {LaunchShape{false, sep, 256, 1024, 2}, LaunchShape{false, sep, 256, 1024, 4},
                                  LaunchShape{false, sep, 256, 256, 1}, LaunchShape{false, sep, 128, 256, 2},
                                  LaunchShape{true, sep, 256, 4096, 1}, LaunchShape{true, sep, 256, 1024, 1},
-                                 LaunchShape{true, sep, 128, 256, 1}})
+                                 LaunchShape{true, sep, 128, 256, 1}, LaunchShape{true, sep, 256, 256, 1},
+                                 LaunchShape{true, sep, 128, 128, 1}})
       cand_.push_back(s);
     // the fused first-order stage (two blocks of 256 per SM at most)
     if (!dc && b->prec == FVS_PREC_MIXED && fusable(b))
