@@ -255,6 +255,17 @@ def algorithmic_bytes(kernel: str, ncells: int, nedges: int, tsize: int) -> floa
     return 0.0
 
 
+def step_bytes(prec: int) -> int:
+    """Compulsory bytes of an ideally fused LSQ-fn stage per cell (every array
+    read or written once): FP64 state U, U0 read and U written 96 B; cell
+    geometry (3 neighbour ids, centroid, volume); LSQ-fn coefficients (3 x 2);
+    face geometry for 1.5 faces (2 cell ids, normal and length, face centre).
+    FP64 geometry: 96 + 36 + 48 + 72 = 252 B; FP32 geometry (mixed
+    precision): 96 + 24 + 24 + 42 = 186 B."""
+    from fvs2d_gb300 import PREC_MIXED
+    return 186 if prec == PREC_MIXED else 252
+
+
 def run_ours(args) -> dict:
     import numpy as np
 
@@ -312,10 +323,11 @@ def run_ours(args) -> dict:
                 "frac": round(achieved / peak, 4), "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)",
                 "traffic": traffic, "alg_bytes_per_launch": alg, "mean_launch_ms": round(per_launch[dom], 4),
                 "kernel_share": {k: round(v / sum(total.values()), 4) for k, v in total.items()},
-                "step_bytes_model": "252 B per cell-stage (ideal fused LSQ-fn FP64 stage)",
+                "step_bytes_model": f"{step_bytes(prec)} B per cell-stage (ideal fused LSQ-fn stage, "
+                                    f"{'FP32' if prec == PREC_MIXED else 'FP64'} geometry, FP64 state)",
                 "compute_bound": pipe_note(f"{dom}:{args.precision}"),
                 "fp64_pipe_frac": fp64_pipe_frac(f"{dom}:{args.precision}"),
-                "step_frac_of_hbm": round(value / ws * 252 / (peak * 1e9), 4)}
+                "step_frac_of_hbm": round(value / ws * step_bytes(prec) / (peak * 1e9), 4)}
 
     # end to end through the C-ABI with pinned host buffers
     host_u = torch.empty((nc, 4), dtype=torch.float64, pin_memory=True)
