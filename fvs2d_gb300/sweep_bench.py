@@ -325,6 +325,54 @@ def profile_batch(ncases=16, steps=400, chunk=200, fused=False):
     return out
 
 
+def airfoil_shapes(nw=512, nr=256, mach=0.8, aoa=1.25, steps=200):
+    """Per-step device times of the config-3 O-grid (first order, mixed
+    precision): the single-mesh Solver, and a batch of one in a set of launch
+    shapes (persistent or graph of tile launches, separate phases or the fused
+    first-order stage, block / tile / blocks per SM), each after 20 warm-up
+    steps; then the autotuned shape, and the defect-correction iteration with
+    its on-line shape trials over 2,000 steps.  FP64 Solver for reference."""
+    from .batch import Batch
+    from .solver import FvsError, Solver
+    case = sweep.Case(nw, nr, mach, aoa)
+    mesh = case.mesh()
+    out = {"cells": mesh.ncells, "steps": steps}
+    for name, prec in (("solver_mixed", PREC_MIXED), ("solver_fp64", PREC_FP64)):
+        with Solver(mesh, sweep.case_options(case, prec)) as s:
+            s.initialize_solution()
+            s.steps_device(100)
+            out[name + "_us_per_step"] = round(1000.0 * s.steps_device(1000) / 1000, 2)
+    with Batch([mesh], [sweep.case_options(case, PREC_MIXED)]) as b:
+        b.initialize_solution()
+        out["autotune_us_per_step"] = round(1000.0 * b.autotune(3), 2)
+        out["autotuned"] = b.info()
+        b.steps(20)
+        _, ms = b.steps(steps)
+        out["batch_autotuned_us_per_step"] = round(1000.0 * ms / steps, 2)
+        shapes = []
+        for tiled in (False, True):
+            for fused in (False, True):
+                b.set_mode(tiled=tiled, fused=fused, fixed=True)
+                for blk, tile, bps in ((256, 256, 1), (256, 256, 4), (256, 1024, 2), (128, 128, 4), (128, 512, 8),
+                                       (256, 4096, 4)):
+                    r = {"tiled": tiled, "fused": fused, "block": blk, "tile": tile, "blocks_per_sm": bps}
+                    try:
+                        b.set_launch(blk, tile, bps)
+                        b.steps(20)
+                        _, ms = b.steps(steps)
+                        r["us_per_step"] = round(1000.0 * ms / steps, 2)
+                    except FvsError as e:
+                        r["refused"] = str(e)[:80]
+                    shapes.append(r)
+        out["shapes"] = shapes
+        b.set_mode(tiled=True, fused=False, fixed=False)
+        b.set_launch(256, 256, 1)
+        never = np.zeros((1, 4))
+        _, _, _, ms = b.run_to_level(2000, never, 500, dc=True)
+        out["dc_us_per_step"] = round(1000.0 * ms / 2000, 2)
+    return out
+
+
 def main(argv=None):
     import argparse
     ap = argparse.ArgumentParser()
@@ -334,7 +382,12 @@ def main(argv=None):
     ap.add_argument("--profile-batch", action="store_true",
                     help="a fixed 16-case batched run (400 mixed + 400 defect-correction steps) for ncu")
     ap.add_argument("--fused", action="store_true", help="--profile-batch with the fused first-order stage")
+    ap.add_argument("--airfoil-shapes", action="store_true",
+                    help="per-step times of the config-3 O-grid: Solver and a batch of one in its launch shapes")
     a = ap.parse_args(argv)
+    if a.airfoil_shapes:
+        print(json.dumps(airfoil_shapes()), flush=True)
+        return
     if a.profile_batch:
         print(json.dumps(profile_batch(fused=a.fused)), flush=True)
         return
