@@ -138,7 +138,7 @@ struct DevView {
   double gamma = 1.4, khalf = 0, nkhalf = 0, omk = 1, cfl = 1, dt = 0;
   double gm1 = 0.4, igm1 = 2.5, ggm1 = 3.5;  // gamma-1, 1/(gamma-1) and gamma/(gamma-1)
   // the same constants rounded once on the host for the FP32 kernels
-  float fgamma = 1.4f, fgm1 = 0.4f, figm1 = 2.5f, fkhalf = 0, fnkhalf = 0, fomk = 1;
+  float fgamma = 1.4f, fgm1 = 0.4f, figm1 = 2.5f, fkhalf = 0, fnkhalf = 0, fomk = 1, fggm1 = 3.5f;
   // and split into FP32 pairs (hi, lo) for the double-float kernels
   float dgamma[2] = {1.4f, 0}, dgm1[2] = {0.4f, 0}, digm1[2] = {2.5f, 0}, dkhalf[2] = {0, 0}, dnkhalf[2] = {0, 0},
         domk[2] = {1, 0}, dggm1[2] = {3.5f, 0};
@@ -156,7 +156,7 @@ inline void set_fp32_constants(DevView& d) {
     o[1] = float(x - double(o[0]));
   };
   d.fgamma = float(d.gamma); d.fgm1 = float(d.gm1); d.figm1 = float(d.igm1);
-  d.fkhalf = float(d.khalf); d.fnkhalf = float(d.nkhalf); d.fomk = float(d.omk);
+  d.fkhalf = float(d.khalf); d.fnkhalf = float(d.nkhalf); d.fomk = float(d.omk); d.fggm1 = float(d.ggm1);
   split(d.gamma, d.dgamma); split(d.gm1, d.dgm1); split(d.igm1, d.digm1);
   split(d.khalf, d.dkhalf); split(d.nkhalf, d.dnkhalf); split(d.omk, d.domk); split(d.ggm1, d.dggm1);
 }

@@ -2720,19 +2720,89 @@ __device__ __forceinline__ void dc_ghost(const DevView& d, int e, T2 n, const fl
   }
 }
 
+// dual-number helpers of the linearised flux: a*b + c, a*x and x*a for a
+// constant x, and the reciprocal and reciprocal square root from the fast
+// hardware approximations (the tangent only steers the correction; its fixed
+// point is the FP64 residual's whatever the tangent's last bits)
+__device__ __forceinline__ Dual dfma_(Dual a, Dual b, Dual c) {
+  return Dual(fmaf(a.v, b.v, c.v), fmaf(a.d, b.v, fmaf(a.v, b.d, c.d)));
+}
+__device__ __forceinline__ Dual dmulf_(Dual a, float x) { return Dual(a.v * x, a.d * x); }
+__device__ __forceinline__ Dual dfmaf_(Dual a, float x, Dual c) { return Dual(fmaf(a.v, x, c.v), fmaf(a.d, x, c.d)); }
+__device__ __forceinline__ Dual drcp_(Dual a) {
+  const float r = __fdividef(1.0f, a.v);
+  return Dual(r, -a.d * r * r);
+}
+__device__ __forceinline__ Dual drsqrt_(Dual a) {
+  const float r = rsqrtf(a.v);
+  return Dual(r, -0.5f * a.d * r * r * r);
+}
+
+// The Roe flux of roe_flux_area_fp64 (the same folded constants and order)
+// on dual numbers: value and tangent of flux * area in the direction of the
+// primitive tangents.  The value part is the FP32 flux the tangent needs.
+__device__ __forceinline__ void roe_flux_area_dual(float gm1, float ggm1, const Dual* pl, const Dual* pr, float nx,
+                                                   float ny, float af, Dual* flux) {
+  const Dual rhoL = pl[0], uL = pl[1], vL = pl[2], pL = pl[3];
+  const Dual rhoR = pr[0], uR = pr[1], vR = pr[2], pR = pr[3];
+  const Dual riL = drcp_(rhoL), riR = drcp_(rhoR);
+  const Dual unL = dfmaf_(uL, nx, dmulf_(vL, ny)), unR = dfmaf_(uR, nx, dmulf_(vR, ny));
+  const Dual utL = dfmaf_(vL, nx, -dmulf_(uL, ny)), utR = dfmaf_(vR, nx, -dmulf_(uR, ny));
+  const Dual HL = dfma_(dmulf_(pL, ggm1), riL, half(dfma_(uL, uL, vL * vL)));
+  const Dual HR = dfma_(dmulf_(pR, ggm1), riR, half(dfma_(uR, uR, vR * vR)));
+  const Dual sRL = rhoR * riL;
+  const Dual RT = sRL * drsqrt_(sRL);
+  const Dual rho = RT * rhoL;
+  const Dual i1 = drcp_(Dual(1.0f + RT.v, RT.d));
+  const Dual u = dfma_(RT, uR, uL) * i1;
+  const Dual v = dfma_(RT, vR, vL) * i1;
+  const Dual H = dfma_(RT, HR, HL) * i1;
+  const Dual q2 = half(dfma_(u, u, v * v));
+  const Dual a2 = dmulf_(H - q2, gm1);
+  const Dual ra = drsqrt_(a2);
+  const Dual a = a2 * ra, ia2 = ra * ra;
+  const Dual un = dfmaf_(u, nx, dmulf_(v, ny));
+  const Dual ut = dfmaf_(v, nx, -dmulf_(u, ny));
+  const Dual drho = rhoR - rhoL, dp = pR - pL, dun = unR - unL, dut = utR - utL;
+  const Dual rad = rho * a * dun;
+  const Dual hia2 = half(ia2);
+  const Dual L0 = (dp - rad) * hia2;
+  const Dual L1 = rho * dut;
+  const Dual L2 = dfma_(-dp, ia2, drho);
+  const Dual L3 = (dp + rad) * hia2;
+  Dual ws0 = dabs_(un - a), ws3 = dabs_(un + a);
+  const Dual ws1 = dabs_(un);
+  // Harten's fix, 0.5 (l^2 / 0.2 + 0.2) = 2.5 l^2 + 0.1
+  if (ws0.v < 0.2f) ws0 = dfma_(dmulf_(ws0, 2.5f), ws0, Dual(0.1f));
+  if (ws3.v < 0.2f) ws3 = dfma_(dmulf_(ws3, 2.5f), ws3, Dual(0.1f));
+  const Dual w0 = ws0 * L0, w1 = ws1 * L1, w2 = ws1 * L2, w3 = ws3 * L3;
+  const Dual s03 = w0 + w3, sd = s03 + w2, dw = (w3 - w0) * a;
+  // eigenvector sum with tx = -ny, ty = nx
+  const Dual diss1 = dfma_(u, sd, dfmaf_(dw, nx, -dmulf_(w1, ny)));
+  const Dual diss2 = dfma_(v, sd, dfmaf_(dw, ny, dmulf_(w1, nx)));
+  const Dual diss3 = dfma_(H, s03, dfma_(un, dw, dfma_(w1, ut, w2 * q2)));
+  const Dual mL = rhoL * unL, mR = rhoR * unR;
+  const Dual pLR = pL + pR;
+  const float haf = 0.5f * af;
+  flux[0] = dmulf_((mL + mR) - sd, haf);
+  flux[1] = dmulf_(dfma_(mL, uL, mR * uR) + dfmaf_(pLR, nx, -diss1), haf);
+  flux[2] = dmulf_(dfma_(mL, vL, mR * vR) + dfmaf_(pLR, ny, -diss2), haf);
+  flux[3] = dmulf_(dfma_(mL, HL, mR * HR) - diss3, haf);
+}
+
 // tangent of the Roe flux at (pl, pr) in the direction (ql, qr), times the
 // face area
 __device__ __forceinline__ void dc_jvp_core(const DevView& d, const float* pl, const float* ql, const float* pr,
                                             const float* qr, T2 n, float af, float* f) {
-  Dual L[4], R[4], F[4], wsm;
+  Dual L[4], R[4], F[4];
 #pragma unroll
   for (int v = 0; v < 4; v++) {
     L[v] = Dual(pl[v], ql[v]);
     R[v] = Dual(pr[v], qr[v]);
   }
-  roe_flux_fast_t<Dual>(Dual(TP(gamma)), Dual(TP(gm1)), Dual(TP(igm1)), L, R, Dual(n.x), Dual(n.y), F, wsm);
+  roe_flux_area_dual(d.fgm1, d.fggm1, L, R, n.x, n.y, af, F);
 #pragma unroll
-  for (int v = 0; v < 4; v++) f[v] = F[v].d * af;
+  for (int v = 0; v < 4; v++) f[v] = F[v].d;
 }
 
 // J dU of one edge slot (first order: face states are the cell states),
