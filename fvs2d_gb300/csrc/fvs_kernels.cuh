@@ -3126,7 +3126,9 @@ static cudaError_t dc_persistent(const DevView& d, const PersistPlan& p, const D
   return cudaLaunchKernelEx(&cfg, k_persistent_dc<MODE_RK>, d, p, c);
 }
 // one defect-correction step as tile launches (for graph capture)
-__global__ void __launch_bounds__(256) k_tiles_dc_flux(const DevView d, const DcView c, const PersistPlan p) {
+// four blocks of 256 per SM: the dual-number flux fits 64 registers without
+// spilling
+__global__ void __launch_bounds__(256, 4) k_tiles_dc_flux(const DevView d, const DcView c, const PersistPlan p) {
   const int2 tl = p.edge_tiles[blockIdx.x];
   dc_flux_range(d, c, tl.x + threadIdx.x, tl.y, blockDim.x);
 }
