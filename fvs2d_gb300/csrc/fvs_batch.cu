@@ -101,6 +101,7 @@ struct fvs_batch {
   double* d_tile_partials = nullptr;
   double* d_case_norms = nullptr;
   int* d_step0 = nullptr;
+  int* d_case_count = nullptr;  // per active case: tiles of the last stage finished (graph form)
   GridBarrier* d_bar = nullptr;
   int cap_cell_tiles = 0, cap_edge_tiles = 0;
   int norm_cap = 1024;
@@ -207,6 +208,8 @@ int alloc_batch_buffers(fvs_batch* B) {
   B->d_step0 = static_cast<int*>(p);
   ok = ok && B->arena.alloc(p, 16 * (size_t)B->ncases);
   B->d_case_tiles = static_cast<int4*>(p);
+  ok = ok && B->arena.alloc(p, 16 * (size_t)B->ncases);
+  B->d_case_count = static_cast<int*>(p);
   return ok ? FVS_OK : B->fail(FVS_ERR_NOMEM, "device allocation of the batch buffers failed");
 }
 
@@ -300,7 +303,7 @@ int build_plan(fvs_batch* B) {
     if (!B->active[c]) continue;
     const int first = (int)ct.size();
     for (int a = B->coff[c]; a < B->coff[c] + B->cnum[c]; a += B->tile)
-      ct.push_back(make_int4(a, std::min(a + B->tile, B->coff[c] + B->cnum[c]), c, 0));
+      ct.push_back(make_int4(a, std::min(a + B->tile, B->coff[c] + B->cnum[c]), c, (int)cases.size()));
     for (int a = B->eoff[c]; a < B->eoff[c] + B->enumv[c]; a += B->tile)
       et.push_back(make_int2(a, std::min(a + B->tile, B->eoff[c] + B->enumv[c])));
     cases.push_back(make_int4(c, first, (int)ct.size(), B->cnum[c]));
@@ -337,6 +340,7 @@ int build_plan(fvs_batch* B) {
   P.nedge_tiles = (int)et.size();
   P.case_tiles = B->d_case_tiles;
   P.ncase_active = (int)cases.size();
+  P.case_count = B->d_case_count;
   P.tile_partials = B->d_tile_partials;
   P.case_norms = B->d_case_norms;
   P.norm_cap = B->norm_cap;
@@ -378,6 +382,7 @@ int launch_chunk(fvs_batch* B, int nsteps, int step0, bool timed = false) {
       if (e != cudaSuccess) return B->cuda_fail(e, "tiled step capture");
     }
     e = cudaMemsetAsync(B->d_bar, 0, sizeof(GridBarrier), B->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(B->d_case_count, 0, sizeof(int) * (size_t)B->ncases, B->stream);
     if (timed) cudaEventRecord(B->eva, B->stream);
     for (int i = 0; i < nsteps && e == cudaSuccess; i++) e = cudaGraphLaunch(B->tgraph, B->stream);
     if (timed) cudaEventRecord(B->evb, B->stream);
@@ -995,6 +1000,7 @@ int fvs_batch_run_to_level_dc(fvs_batch* b, int32_t max_steps, const double* lev
     *b->h_step0 = step;
     e = cudaMemcpyAsync(b->d_step0, b->h_step0, sizeof(int), cudaMemcpyHostToDevice, b->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(b->d_bar, 0, sizeof(GridBarrier), b->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(b->d_case_count, 0, sizeof(int) * (size_t)b->ncases, b->stream);
     if (b->tiled) {
       b->plan.nsteps = 1;
       if (e == cudaSuccess && !b->tgraph_dc)

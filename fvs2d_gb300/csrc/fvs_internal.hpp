@@ -263,7 +263,9 @@ struct PersistPlan {
   int nedge_tiles = 0;
   int tile = 0;                          // tile length (cells or edge slots)
   const int4* case_tiles = nullptr;      // x = case, y = first cell tile, z = end tile, w = cells of the case
+                                         // (cell_tiles[t].w = the index of t's case in case_tiles)
   int ncase_active = 0;
+  int* case_count = nullptr;             // [case_tiles] tiles of the step's last stage done (graph form)
   double* tile_partials = nullptr;       // [ncell_tiles][4]
   double* case_norms = nullptr;          // [ncases][norm_cap][4]
   int norm_cap = 0;

@@ -2254,6 +2254,39 @@ __device__ __forceinline__ void case_norms_of_step(const PersistPlan& p, int ste
   }
 }
 
+// Graph form, last stage: the block that finishes the last tile of a case
+// (a counter per case) sums that case's norm from its tile partials; the
+// last case of the step advances the device step counter.  This replaces a
+// separate norm launch per step (~8 us of a 64 us step on a single
+// 261,120-cell case).  Call after the tile's partial is written; every
+// thread of the block calls it.
+__device__ __forceinline__ void tiled_case_norm(const PersistPlan& p, int t) {
+  __shared__ int s_last;
+  const int slot = p.cell_tiles[t].w;
+  const int4 ct = p.case_tiles[slot];
+  if (threadIdx.x == 0) {
+    __threadfence();
+    s_last = atomicAdd(&p.case_count[slot], 1) == ct.z - ct.y - 1;
+  }
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  double a[4];
+  case_tile_sum(p, ct, a);
+  if (threadIdx.x == 0) {
+    const int step = __ldcg(p.step0_dev);
+    double* o = p.case_norms + 4 * ((size_t)ct.x * p.norm_cap + step % p.norm_cap);
+#pragma unroll
+    for (int k = 0; k < 4; k++) o[k] = sqrt(a[k] / double(ct.w));
+    p.case_count[slot] = 0;
+    __threadfence();
+    if (atomicAdd(&p.bar->count, 1u) == (unsigned)p.ncase_active - 1) {
+      p.bar->count = 0u;
+      *const_cast<int*>(p.step0_dev) = step + 1;
+    }
+  }
+}
+
 template <int LIM, int REC>
 __global__ void __launch_bounds__(256) k_persistent(const DevView d, const PersistPlan p) {
   const int nb = gridDim.x;
@@ -2426,6 +2459,7 @@ template <int MODE>
 __global__ void __launch_bounds__(256, 2) k_tiles_cell(const DevView d, const PersistPlan p, int k) {
   const double time = p.t1 + double(*p.step0_dev) * d.dt + p.sp[k].dts;
   cell_stage_tile<MODE>(d, p, p.sp[k], stage_pin(d, k), stage_pout(d, k), blockIdx.x, time);
+  if (p.sp[k].last) tiled_case_norm(p, blockIdx.x);
 }
 #endif
 
@@ -2519,38 +2553,17 @@ __global__ void __launch_bounds__(256) k_tiles_flux(const DevView d, const Persi
 
 template <int MODE, bool ONE>
 __global__ void __launch_bounds__(256) k_tiles_update(const DevView d, const PersistPlan p, int stage) {
+  const StageParams& sp = p.sp[stage];
   if (ONE) {
-    const StageParams& sp = p.sp[stage];
     const int4 tl = p.cell_tiles[blockIdx.x];
     const int ic = tl.x + threadIdx.x;
     NormAcc na;
     if (ic < tl.y) update_item<MODE, false>(d, sp, ic, na);
     if (sp.last) tile_norm_partial(p, na, blockIdx.x);
   } else {
-    update_tile<MODE>(d, p, p.sp[stage], blockIdx.x);
+    update_tile<MODE>(d, p, sp, blockIdx.x);
   }
-}
-
-// per-case RMS of the step from the tile partials (fixed order), one block
-// per active case, of the batch's block size (the persistent kernel's order);
-// the last block to finish advances the step counter
-__global__ void __launch_bounds__(256) k_tiles_norms(const PersistPlan p) {
-  __shared__ int s_last;
-  const int step = *p.step0_dev;
-  const int4 ct = p.case_tiles[blockIdx.x];
-  double a[4];
-  case_tile_sum(p, ct, a);
-  if (threadIdx.x == 0) {
-    double* o = p.case_norms + 4 * ((size_t)ct.x * p.norm_cap + step % p.norm_cap);
-#pragma unroll
-    for (int k = 0; k < 4; k++) o[k] = sqrt(a[k] / double(ct.w));
-    __threadfence();
-    s_last = atomicAdd(&p.bar->count, 1u) == gridDim.x - 1;
-    if (s_last) {
-      p.bar->count = 0u;
-      *const_cast<int*>(p.step0_dev) = step + 1;
-    }
-  }
+  if (sp.last) tiled_case_norm(p, blockIdx.x);
 }
 
 static cudaError_t launch_tiled_step(const DevView& d, const PersistPlan& p, int block, cudaStream_t s) {
@@ -2564,7 +2577,6 @@ static cudaError_t launch_tiled_step(const DevView& d, const PersistPlan& p, int
         default: k_tiles_cell<MODE_RK><<<p.ncell_tiles, block, 0, s>>>(d, p, k); break;
       }
     }
-    k_tiles_norms<<<p.ncase_active, block, 0, s>>>(p);
     return cudaGetLastError();
   }
 #endif
@@ -2593,7 +2605,6 @@ static cudaError_t launch_tiled_step(const DevView& d, const PersistPlan& p, int
       default: k_tiles_update<MODE_RK, false><<<p.ncell_tiles, block, 0, s>>>(d, p, k); break;
     }
   }
-  k_tiles_norms<<<p.ncase_active, block, 0, s>>>(p);
   return cudaGetLastError();
 }
 
@@ -3137,6 +3148,7 @@ template <int MODE, bool FUSED>
 __global__ void __launch_bounds__(256) k_tiles_dc_update(const DevView d, const DcView c, const PersistPlan p,
                                                          int stage) {
   dc_stage_tile<MODE, FUSED>(d, c, p, stage, blockIdx.x);
+  if (p.sp[stage].last) tiled_case_norm(p, blockIdx.x);
 }
 
 static cudaError_t dc_tiled_step(const DevView& d, const PersistPlan& p, const DcView& c, int block, cudaStream_t s) {
@@ -3150,7 +3162,6 @@ static cudaError_t dc_tiled_step(const DevView& d, const PersistPlan& p, const D
     if (p.sp[k].mode == MODE_SSP42) k_tiles_dc_update<MODE_SSP42, false><<<p.ncell_tiles, block, 0, s>>>(d, c, p, k);
     else k_tiles_dc_update<MODE_RK, false><<<p.ncell_tiles, block, 0, s>>>(d, c, p, k);
   }
-  k_tiles_norms<<<p.ncase_active, block, 0, s>>>(p);
   return cudaGetLastError();
 }
 #endif  // FVS_MIXED
