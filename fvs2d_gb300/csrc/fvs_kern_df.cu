@@ -1,6 +1,7 @@
 // fvs_kern_df.cu — device kernels, FP64 accuracy on the FP32 pipe: gradient,
-// limiter, reconstruction, Roe flux and the slot gather in double-float (df64,
-// 48-bit significand); FP64 state update, local time step and norms.
+// limiter, reconstruction, Roe flux, the slot gather and the RK stage in
+// double-float (df64, 48-bit significand); the state stored in FP64, FP64
+// local time step, norms summed as FP32 pairs.
 #define FVS_NS k_df
 #define FVS_T df64
 #define FVS_MIXED 0

@@ -1,5 +1,6 @@
 // fvs_kern_mixed.cu — device kernels, mixed precision: FP32 gradient, limiter, reconstruction and Roe flux;
-// FP64 residual accumulation, state update, local time step and norms.
+// residual sums exact (TwoSum), the RK increment in FP32 added to the FP64 state, FP64 local time step, norms
+// summed as FP32 pairs.
 #define FVS_NS k_mixed
 #define FVS_T float
 #define FVS_MIXED 1
